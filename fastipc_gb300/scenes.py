@@ -90,6 +90,10 @@ class Scene:
     gravity: float = -9.8
     steps: int = 50
     meta: dict = field(default_factory=dict)
+    x_init: np.ndarray = None     # [V,3] initial positions when they differ from the rest shape
+
+    def initial_positions(self):
+        return self.x if self.x_init is None else self.x_init
 
     @property
     def n_verts(self):
@@ -200,6 +204,16 @@ def twisted_bar(nx=400, ny=20, nz=20, size=(1.0, 0.05, 0.05), seed=0, jitter=1e-
                    steps=steps, meta={'seed': seed, 'nx': nx, 'ny': ny, 'nz': nz})
 
 
-def small_two_cubes(n=3, seed=0, **kw):
-    """two_cubes with few hexes: the case the pure-python reference run can finish."""
-    return two_cubes(n=n, seed=seed, **kw)
+def predeform(scene, amplitude, seed=0):
+    """Start ``scene`` from its rest shape plus seeded uniform +-amplitude displacements on
+    the free vertices.  At an exactly undeformed element the reference's projected
+    Neo-Hookean Hessian depends on the sign of rounding noise (its 2x2 make_pd acts on the
+    twist/flip blocks only when a coefficient is negative), so states used for
+    iteration-by-iteration parity start away from rest."""
+    rng = np.random.default_rng(seed + 7919)
+    mask, _ = scene.dirichlet(0.0)
+    d = rng.uniform(-amplitude, amplitude, scene.x.shape)
+    d[mask] = 0.0
+    scene.x_init = scene.x + d
+    scene.meta['predeform'] = amplitude
+    return scene

@@ -303,13 +303,14 @@ def gen_cube_mesh():
 def gen_newton(n=3, steps=6, seed=0, record_iters=11, matrix_iters=(0, 2, 5)):
     """Run NEWTON_IPC.py's own functions on a small two-cube scene and record every step.
 
+    The scene starts pre-deformed by +-0.5 mm (scenes.predeform).
     Source edits (the same ones the CPU-baseline notes list): Neo-Hookean import instead of
     fixed-corotated, dt = 0.01, E = 1e5, nu = 0.4, smaller MAX_LINEAR/MAX_C buffers.
     d-hat^2 stays 1e-6 (d-hat = 1e-3 m, as in the two-cube scene).  The driver loop below
     follows NEWTON_IPC.py:955-996 statement by statement, calling the module's functions.
     """
     from fastipc_gb300 import scenes
-    scene = scenes.two_cubes(n=n, seed=seed)
+    scene = scenes.predeform(scenes.two_cubes(n=n, seed=seed), 5e-4, seed)
     subs = [
         ('from common.physics.fixed_corotated import *', 'from common.physics.neo_hookean import *'),
         ('dt = 0.04', 'dt = 0.01'),
@@ -356,7 +357,10 @@ def gen_newton(n=3, steps=6, seed=0, record_iters=11, matrix_iters=(0, 2, 5)):
     R.kappa = R.compute_adaptive_kappa() * 10
     R.spatial_hash_inv_dx = 1.0 / R.compute_mean_of_boundary_edges()
     R.save_x0()
-    rec = {'x_init': scene.x, 'v_init': scene.v, 'tets': scene.tets,
+    # start from the pre-deformed state (rest shape, x0, kappa and the hash cell keep the
+    # rest positions); see scenes.predeform for why
+    R.x.from_numpy(scene.initial_positions().astype(np.float64))
+    rec = {'x_init': scene.initial_positions(), 'x_rest': scene.x, 'predeform': 5e-4, 'v_init': scene.v, 'tets': scene.tets,
            'bpoints': scene.boundary_points, 'bedges': scene.boundary_edges, 'btris': scene.boundary_triangles,
            'kappa': R.kappa, 'inv_dx': R.spatial_hash_inv_dx, 'mass': R.m.to_numpy(),
            'dt': R.dt, 'dhat2': R.dHat2, 'n': n, 'seed': seed, 'steps': steps}

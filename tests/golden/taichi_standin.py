@@ -84,7 +84,8 @@ class Mat(np.ndarray):
     """Taichi small matrix/vector value (1-D array = column vector)."""
 
     def __new__(cls, data):
-        return np.asarray(data, dtype=np.float64).view(cls)
+        # taichi matrices are values: always copy so in-place edits never alias the input
+        return np.array(data, dtype=np.float64).view(cls)
 
     @property
     def n(self):
@@ -162,7 +163,7 @@ class Matrix:
 
 class Vector:
     def __new__(cls, data):
-        a = np.asarray(data)
+        a = np.array(data)
         if a.dtype.kind in 'iu':          # integer vectors (index tuples) stay integer
             return a.view(Mat)
         return Mat(a.astype(np.float64))
