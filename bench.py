@@ -1,0 +1,315 @@
+"""Benchmark: steps/s and ms per Newton iteration of the IPC Newton loop on the 960k-tet twisted bar.
+
+Workload: a 0.05 x 0.05 x 1.0 m bar, 20 x 20 x 400 hexes x 6 tets (176,841 vertices, 960,000
+tets), Neo-Hookean E = 1e6 Pa, nu = 0.45, rho = 1000, d-hat = 5e-4 m, dt = 0.01 s, both end faces
+Dirichlet and rotating at +-pi rad/s, seed-drawn +-1e-4 m jitter: synthetic data generated here.
+A step is one implicit time step (the full Newton loop with CCD line search).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nx 400]
+
+Ours: W warm-up steps, then K steps timed with CUDA events on the simulation stream between a
+barrier + synchronize on both sides (max over ranks); `value` = N*K / max time.  `e2e` re-runs
+the same K steps from the same state through the C-ABI path with the state copied from pinned
+host memory before each step and read back after it.  With --gpus N > 1 (torchrun) every rank
+runs an independent replica: the path has no data-parallel shard (one scene, one GPU).
+
+Reference arm (--impl reference): the CPU oracle's implementation of the same Newton path
+(C/OpenMP kernels + block-Jacobi PCG, all host cores), timed on whole time steps of the same
+scene; rank 0 only.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = 'steps/s (twisted bar, 960k tets)'
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--nx', type=int, default=400, help='hexes along the bar (400 = the 960k-tet configuration)')
+    ap.add_argument('--pcg-rtol', type=float, default=1e-6)
+    ap.add_argument('--profile-kernel', type=int, default=1, help='kernel timed for the roofline (1 = PCG SpMV)')
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--cpu-sample-pcg', type=int, default=100000)
+    return ap.parse_args()
+
+
+def make_scene(nx):
+    from fastipc_gb300 import scenes
+    return scenes.twisted_bar(nx=nx, ny=20, nz=20, size=(nx / 400.0, 0.05, 0.05), seed=0)
+
+
+def workload(nx, pcg_rtol):
+    return {'workload': f'twisted bar {nx}x20x20 hexes x6 tets ({nx * 2400} tets), NH E=1e6 nu=0.45, dhat=5e-4, dt=0.01',
+            'tets': nx * 2400, 'verts': (nx + 1) * 441, 'newton_tol': '|p|inf < 1e-2 dt', 'pcg_rtol': pcg_rtol,
+            'l2': 'inputs larger than L2 (element Hessians alone ~0.7 GB per Newton iteration)'}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix='.csv')
+        os.close(fd)
+        q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,'
+             'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+        try:
+            self.proc = subprocess.Popen(['nvidia-smi', f'--id={self.index}', f'--query-gpu={q}', '--format=csv,noheader,nounits',
+                                          '-lms', '200'], stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+
+    def summary(self):
+        import statistics
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(',')]
+                if len(f) >= 9 and f[1].isdigit():
+                    rows.append(f)
+        except OSError:
+            pass
+        if not rows:
+            return {'sm_mhz': None, 'sm_max_mhz': None, 'reasons': ['unsampled']}
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        return {'sm_mhz': statistics.median(int(r[1]) for r in rows), 'sm_max_mhz': int(rows[0][2]),
+                'power_w_max': max(float(r[3]) for r in rows if r[3].replace('.', '').isdigit()) if rows else None,
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(HERE, 'MEASURED_PEAKS.json'))), 'measured'
+    except (OSError, ValueError):
+        return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0}, 'fallback'
+
+
+def ncu_traffic(kernel_id):
+    """dram bytes per launch of the profiled kernel from a committed ncu capture, if any."""
+    name = {1: 'pcg_spmv', 2: 'pcg_update', 3: 'nh_element'}.get(kernel_id)
+    path = os.path.join(HERE, 'profiles', f'{name}_traffic.json')
+    try:
+        d = json.load(open(path))
+        return float(d['dram_bytes_per_launch_scaled']), d.get('note')
+    except (OSError, ValueError, KeyError):
+        return None, None
+
+
+def cpu_baseline(scene, newton_per_step, pcg_per_newton, args):
+    """The oracle on the host cores: one Newton iteration of time step 1 of the same scene
+    (constraints, assembly, full PCG solve, line search), scaled to steps/s with the Newton and
+    PCG iteration counts of the timed GPU steps (the same algorithm)."""
+    from oracle import oracle as O
+    sim = O.OracleSim(scene, solver='bsr', pcg_rtol=args.pcg_rtol, pcg_maxit=args.cpu_sample_pcg)
+    sim.step(0, max_newton=1)                 # rest state (zero right-hand side)
+    sim.timings = {}
+    t0 = time.perf_counter()
+    sim.compute_xn_and_xTilde()
+    sim.move_nodes(1 * sim.dt)
+    sim.find_constraints()
+    sim.compute_hessian_and_gradient()
+    t1 = time.perf_counter()
+    sim.solve_system(1 * sim.dt)
+    t2 = time.perf_counter()
+    E0 = sim.compute_energy()
+    sim.xPrev = sim.x.copy()
+    alpha = sim.compute_intersection_free_step_size()
+    sim.apply_sol(alpha)
+    sim.check_collision()
+    sim.find_constraints()
+    sim.compute_energy()
+    t3 = time.perf_counter()
+    pcg_its = max(sim.pcg_iters[-1], 1)
+    t_fixed = (t1 - t0) + (t3 - t2)
+    t_pcg_it = (t2 - t1) / pcg_its
+    t_newton = t_fixed + t_pcg_it * pcg_per_newton
+    sps = 1.0 / (t_newton * newton_per_step)
+    _ = E0
+    return {'value': sps, 'unit': 'steps/s', 'cores': O.lib().oracle_num_threads(), 'kind': 'port',
+            'sample': (f'one Newton iteration of step 1 of the same scene on the host cores ({t3 - t0:.1f} s: '
+                       f'assembly+constraints+line search {t_fixed:.2f} s, PCG {pcg_its} its at {1e3 * t_pcg_it:.2f} ms/it); '
+                       f'scaled by the timed GPU steps\' {newton_per_step:.2f} Newton its/step and {pcg_per_newton:.0f} PCG its/Newton'),
+            'ms_per_newton_iter': 1e3 * t_newton}
+
+
+def run_reference(args):
+    """CPU oracle, whole time steps of the same scene (rank 0 only)."""
+    rank = int(os.environ.get('RANK', '0'))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    scene = make_scene(args.nx)
+    sim = O.OracleSim(scene, solver='bsr', pcg_rtol=args.pcg_rtol, pcg_maxit=args.cpu_sample_pcg)
+    f = 0
+    for _ in range(args.warmup):
+        sim.step(f)
+        f += 1
+    t0 = time.perf_counter()
+    n0 = len(sim.newton_iters)
+    for _ in range(args.steps):
+        sim.step(f)
+        f += 1
+    dt = time.perf_counter() - t0
+    its = sim.newton_iters[n0:]
+    v = args.steps / dt
+    out = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'steps/s', 'n_gpus': args.gpus, 'steps': args.steps,
+           'warmup': args.warmup, 'ms_per_step': 1e3 * dt / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload(args.nx, args.pcg_rtol),
+           'ms_per_newton_iter': 1e3 * dt / max(sum(its), 1), 'newton_iters_per_step': sum(its) / len(its),
+           'cpu_baseline': {'value': v, 'unit': 'steps/s', 'cores': O.lib().oracle_num_threads(), 'kind': 'port',
+                            'sample': f'{args.steps} whole time steps ({args.warmup}..{args.warmup + args.steps - 1}) of the same scene'},
+           'e2e': {'value': v, 'unit': 'steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    import numpy as np
+    import torch
+    from fastipc_gb300 import _native
+    from fastipc_gb300.build import build
+    from fastipc_gb300.newton import NewtonIPC
+
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    build()
+    scene = make_scene(args.nx)
+    sim = NewtonIPC(scene, device=dev, pcg_rtol=args.pcg_rtol)
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    f = 0
+    for _ in range(args.warmup):
+        sim.step(f)
+        f += 1
+    snap = (sim.x.clone(), sim.v.clone())
+    f0 = f
+    n_newton0, n_pcg0 = len(sim.newton_iters), len(sim.pcg_iters)
+    L = _native.lib()
+    L.fipc_profile_enable(args.profile_kernel)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _native.launch_count()
+    barrier()
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.step(f)
+            f += 1
+        ev1.record(stream)
+        barrier()
+    launches = _native.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    pt, pn, pb, pf = ctypes_read(L)
+    L.fipc_profile_enable(0)
+    newton = sim.newton_iters[n_newton0:]
+    pcg = sim.pcg_iters[n_pcg0:]
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * args.steps / (ms_max / 1e3)
+
+    # e2e: the same steps again from the same state, state round-tripped through pinned host memory
+    hx = torch.empty_like(snap[0], device='cpu').pin_memory()
+    hv = torch.empty_like(snap[1], device='cpu').pin_memory()
+    hx.copy_(snap[0])
+    hv.copy_(snap[1])
+    sim.newton_iters, sim.pcg_iters = [], []
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    f = f0
+    for _ in range(args.steps):
+        sim.x.copy_(hx, non_blocking=True)
+        sim.v.copy_(hv, non_blocking=True)
+        sim.step(f)
+        hx.copy_(sim.x, non_blocking=True)
+        hv.copy_(sim.v, non_blocking=True)
+        f += 1
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist is not None:
+        t = torch.tensor([e2e_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    nbytes = 2 * sim.x.numel() * 8
+
+    if rank == 0:
+        pk, src = peaks()
+        achieved = pb / (pt / 1e3) / 1e9 if pt > 0 else None
+        traffic, note = ncu_traffic(args.profile_kernel)
+        newton_per_step = sum(newton) / len(newton)
+        pcg_per_newton = sum(pcg) / max(len(pcg), 1)
+        roof = {'kernel': {1: 'k_pcg_spmv', 2: 'k_pcg_update', 3: 'k_elasticity'}.get(args.profile_kernel),
+                'bound': 'hbm', 'achieved': achieved, 'peak': pk['hbm_gbs'], 'unit': 'GB/s',
+                'frac': achieved / pk['hbm_gbs'] if achieved else None,
+                'traffic': traffic * 1.0 if traffic is not None else None,
+                'algorithmic_bytes_per_launch': pb / max(pn, 1), 'avg_launch_us': 1e3 * pt / max(pn, 1), 'launches': pn,
+                'peak_source': src, 'time_share_of_step': pt / ms if ms > 0 else None}
+        if note:
+            roof['traffic_note'] = note
+        out = {'metric': METRIC, 'value': value, 'unit': 'steps/s', 'n_gpus': world, 'steps': args.steps,
+               'warmup': args.warmup, 'ms_per_step': ms_max / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+               'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload(args.nx, args.pcg_rtol),
+               'ms_per_newton_iter': ms_max / max(sum(newton), 1), 'newton_iters_per_step': newton_per_step,
+               'pcg_iters_per_newton': pcg_per_newton, 'parallelism': 'replicas' if world > 1 else 'single',
+               'e2e': {'value': world * args.steps / (e2e_ms / 1e3), 'unit': 'steps/s', 'h2d_bytes_per_step': nbytes,
+                       'd2h_bytes_per_step': nbytes},
+               'gpu_launches': launches, 'roofline': roof, 'clocks': clk.summary(),
+               'sections_s': {k: round(v, 4) for k, v in sim.timer.total.items()}}
+        if world == 1 and not args.no_cpu_baseline:
+            out['cpu_baseline'] = cpu_baseline(scene, newton_per_step, pcg_per_newton, args)
+        print(json.dumps(out), flush=True)
+    sim.close()
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def ctypes_read(L):
+    import ctypes
+    t, n, b, fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double(), ctypes.c_double()
+    L.fipc_profile_read(ctypes.byref(t), ctypes.byref(n), ctypes.byref(b), ctypes.byref(fl))
+    return t.value, n.value, b.value, fl.value
+
+
+if __name__ == '__main__':
+    main()

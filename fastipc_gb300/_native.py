@@ -1,0 +1,81 @@
+"""ctypes binding of libfastipc.so (include/fastipc.h).
+
+The library is the only compute path: importing this module never falls back to anything
+else, and every entry point raises ``FastIPCError`` when the library is missing or a call
+returns a non-zero status.
+"""
+import ctypes
+import os
+
+from .build import LIB
+
+_lib = None
+
+STATUS = {0: 'ok', 1: 'capacity exceeded', 2: 'iteration limit reached', 3: 'non-finite value', 4: 'CUDA error',
+          5: 'invalid argument'}
+
+# symbols declared in include/fastipc.h
+EXPORTS = [
+    'fipc_elasticity', 'fipc_barrier_rows', 'fipc_ccd_pairs', 'fipc_inversion_free_pairs', 'fipc_compute_xn_and_xtilde',
+    'fipc_move_nodes', 'fipc_apply_sol', 'fipc_compute_v', 'fipc_ctx_create', 'fipc_ctx_destroy', 'fipc_ctx_params',
+    'fipc_ctx_set_params', 'fipc_ctx_mass', 'fipc_ctx_set_x0', 'fipc_find_constraints', 'fipc_get_constraints',
+    'fipc_compute_hessian_and_gradient', 'fipc_system_sizes', 'fipc_export_system', 'fipc_solve_system',
+    'fipc_output_residual', 'fipc_compute_energy', 'fipc_compute_intersection_free_step_size', 'fipc_check_collision',
+    'fipc_launch_count', 'fipc_status_string', 'fipc_profile_enable', 'fipc_profile_read',
+]
+
+
+class FastIPCError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__(f'{what}: {STATUS.get(status, status)} (status {status})')
+
+
+def lib():
+    """Load libfastipc.so (built by fastipc_gb300.build.build())."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            raise FastIPCError(4, f'libfastipc.so not built at {LIB}; run fastipc_gb300.build.build()')
+        L = ctypes.CDLL(LIB)
+        for name in EXPORTS:
+            getattr(L, name).restype = ctypes.c_int
+        L.fipc_launch_count.restype = ctypes.c_longlong
+        L.fipc_status_string.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def check(status, what):
+    if status != 0:
+        raise FastIPCError(status, what)
+
+
+def dptr(t, dtype=None):
+    """Device pointer of a contiguous CUDA tensor (checked)."""
+    import torch
+    if t is None:
+        return None
+    if not t.is_cuda:
+        raise FastIPCError(5, 'expected a CUDA tensor')
+    if not t.is_contiguous():
+        raise FastIPCError(5, 'expected a contiguous tensor')
+    if dtype is not None and t.dtype != dtype:
+        raise FastIPCError(5, f'expected dtype {dtype}, got {t.dtype}')
+    _ = torch
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def hptr(a):
+    """Host pointer of a contiguous numpy array."""
+    assert a.flags['C_CONTIGUOUS']
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def stream():
+    import torch
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def launch_count():
+    return int(lib().fipc_launch_count())

@@ -1,0 +1,587 @@
+// Sort-based spatial hash and the three queries built on it: constraint finding
+// (NEWTON_IPC.py:181-357), the CCD step filter (NEWTON_IPC.py:377-468) and the
+// intersection check (NEWTON_IPC.py:855-886).
+//
+// The grid has the reference's cell size (1 / inv_dx, the mean boundary edge) and the same
+// box conventions: what the reference appends to its sparse grid becomes (cell key, id)
+// pairs, radix-sorted by key; unique keys and run starts give each cell's id range, found by
+// binary search.  A candidate pair whose two cell ranges overlap in several cells is examined
+// only in the overlap's lowest cell (componentwise max of the two lower corners), so every
+// pair is tested once without a hash set.  The narrow phase applies the reference's exact
+// predicates; constraint rows are then sorted lexicographically and de-duplicated per list
+// exactly like np.unique(axis=0) (NEWTON_IPC.py:348-356).
+#include <cub/cub.cuh>
+#include <cuda_runtime.h>
+
+#include "ccd.cuh"
+#include "ctx.cuh"
+#include "geometry.cuh"
+
+namespace fipc {
+
+struct C3 {
+    long long x, y, z;
+};
+
+__device__ __forceinline__ C3 cell_of(v3 p, double inv_dx) {
+    return C3{(long long)floor(p.x * inv_dx), (long long)floor(p.y * inv_dx), (long long)floor(p.z * inv_dx)};
+}
+__device__ __forceinline__ C3 cmax(C3 a, C3 b) { return C3{a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z}; }
+
+// Box modes of stored primitives:
+//  0 point [p - dh, p + dh]               (find constraints, point-triangle)
+//  1 edge  [min, max]                      (find constraints, edge-edge)
+//  2 moving point [min(p, p+dp) - dh, max + dh]   (CCD point-triangle)
+//  3 moving edge  [min over 4 ends, max]           (CCD edge-edge)
+//  4 edge  [min - dh, max + dh]            (intersection check)
+__device__ __forceinline__ void stored_box(int mode, int i, const int* __restrict__ prim, const double* __restrict__ x,
+                                           const double* __restrict__ p, double dh, v3* lo, v3* hi) {
+    if (mode == 0 || mode == 2) {
+        const v3 a = ld3(x, prim[i]);
+        v3 mn = a, mx = a;
+        if (mode == 2) {
+            const v3 b = a + ld3(p, prim[i]);
+            mn = vmin(a, b);
+            mx = vmax(a, b);
+        }
+        *lo = mn - mk(dh, dh, dh);
+        *hi = mx + mk(dh, dh, dh);
+    } else {
+        const v3 a = ld3(x, prim[2 * i]), b = ld3(x, prim[2 * i + 1]);
+        v3 mn = vmin(a, b), mx = vmax(a, b);
+        if (mode == 3) {
+            const v3 a2 = a + ld3(p, prim[2 * i]), b2 = b + ld3(p, prim[2 * i + 1]);
+            mn = vmin(mn, vmin(a2, b2));
+            mx = vmax(mx, vmax(a2, b2));
+        }
+        if (mode == 4) {
+            mn = mn - mk(dh, dh, dh);
+            mx = mx + mk(dh, dh, dh);
+        }
+        *lo = mn;
+        *hi = mx;
+    }
+}
+
+constexpr long long MAX_CELLS_PER_PRIM = 1ll << 22;
+
+__global__ void k_cell_count(int mode, int n, const int* __restrict__ prim, const double* __restrict__ x,
+                             const double* __restrict__ p, double dh, double inv_dx, long long* __restrict__ cnt,
+                             int* __restrict__ overflow) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    v3 lo, hi;
+    stored_box(mode, i, prim, x, p, dh, &lo, &hi);
+    const C3 a = cell_of(lo, inv_dx), b = cell_of(hi, inv_dx);
+    long long c = (b.x - a.x + 1) * (b.y - a.y + 1) * (b.z - a.z + 1);
+    if (!(c > 0 && c <= MAX_CELLS_PER_PRIM)) {
+        atomicOr(overflow, 1);
+        c = 0;
+    }
+    cnt[i] = c;
+}
+
+__global__ void k_cell_emit(int mode, int n, const int* __restrict__ prim, const double* __restrict__ x,
+                            const double* __restrict__ p, double dh, double inv_dx, const long long* __restrict__ off,
+                            const long long* __restrict__ cnt, unsigned long long* __restrict__ keys, int* __restrict__ ids) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || cnt[i] == 0) return;
+    v3 lo, hi;
+    stored_box(mode, i, prim, x, p, dh, &lo, &hi);
+    const C3 a = cell_of(lo, inv_dx), b = cell_of(hi, inv_dx);
+    long long o = off[i];
+    for (long long cx = a.x; cx <= b.x; ++cx)
+        for (long long cy = a.y; cy <= b.y; ++cy)
+            for (long long cz = a.z; cz <= b.z; ++cz) {
+                keys[o] = cell_key(cx, cy, cz);
+                ids[o] = i;
+                ++o;
+            }
+}
+
+// position of key in the sorted unique keys, or -1
+__device__ __forceinline__ int find_cell(const unsigned long long* __restrict__ uk, int nu, unsigned long long key) {
+    int lo = 0, hi = nu;
+    while (lo < hi) {
+        const int m = (lo + hi) >> 1;
+        if (__ldg(uk + m) < key) lo = m + 1;
+        else hi = m;
+    }
+    return (lo < nu && __ldg(uk + lo) == key) ? lo : -1;
+}
+
+// ---------------------------------------------------------------- constraint rows
+struct RowSink {
+    int4* rows[N_TYPES];
+    int* counts;   // [N_TYPES + 1]; the last entry is the overflow flag
+    int cap;
+};
+__device__ __forceinline__ void emit(const RowSink& s, int t, int a, int b, int c, int d) {
+    const int k = atomicAdd(&s.counts[t], 1);
+    if (k < s.cap) s.rows[t][k] = make_int4(a, b, c, d);
+    else atomicOr(&s.counts[N_TYPES], 1);
+}
+
+// attempt_PT, NEWTON_IPC.py:181-212
+__device__ void attempt_pt(const double* __restrict__ x, double dh, double dh2, int p, int t0, int t1, int t2, const RowSink& s) {
+    if (p == t0 || p == t1 || p == t2) return;
+    const v3 P = ld3(x, p), A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
+    if (!pt_aabb(P, A, B, C, dh)) return;
+    switch (pt_type(P, A, B, C)) {
+        case 0: if (d_PP(P, A) < dh2) emit(s, T_PP, p, t0, 0, 0); break;
+        case 1: if (d_PP(P, B) < dh2) emit(s, T_PP, p, t1, 0, 0); break;
+        case 2: if (d_PP(P, C) < dh2) emit(s, T_PP, p, t2, 0, 0); break;
+        case 3: if (d_PE(P, A, B) < dh2) emit(s, T_PE, p, t0, t1, 0); break;
+        case 4: if (d_PE(P, B, C) < dh2) emit(s, T_PE, p, t1, t2, 0); break;
+        case 5: if (d_PE(P, C, A) < dh2) emit(s, T_PE, p, t2, t0, 0); break;
+        default: if (d_PT(P, A, B, C) < dh2) emit(s, T_PT, p, t0, t1, t2); break;
+    }
+}
+
+// attempt_EE, NEWTON_IPC.py:235-312
+__device__ void attempt_ee(const double* __restrict__ x, const double* __restrict__ x0, double dh, double dh2, int a0, int a1, int b0,
+                           int b1, const RowSink& s) {
+    if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
+    const v3 A0 = ld3(x, a0), A1 = ld3(x, a1), B0 = ld3(x, b0), B1 = ld3(x, b1);
+    if (!ee_aabb(A0, A1, B0, B1, dh)) return;
+    const double ecn = d_EECN2(A0, A1, B0, B1);
+    const double eps = m_threshold(ld3(x0, a0), ld3(x0, a1), ld3(x0, b0), ld3(x0, b1));
+    const bool m = ecn < eps;
+    switch (ee_type(A0, A1, B0, B1)) {
+        case 0: if (d_PP(A0, B0) < dh2) { if (m) emit(s, T_PPM, a0, a1, b0, b1); else emit(s, T_PP, a0, b0, 0, 0); } break;
+        case 1: if (d_PP(A0, B1) < dh2) { if (m) emit(s, T_PPM, a0, a1, b1, b0); else emit(s, T_PP, a0, b1, 0, 0); } break;
+        case 2: if (d_PE(A0, B0, B1) < dh2) { if (m) emit(s, T_PEM, a0, a1, b0, b1); else emit(s, T_PE, a0, b0, b1, 0); } break;
+        case 3: if (d_PP(A1, B0) < dh2) { if (m) emit(s, T_PPM, a1, a0, b0, b1); else emit(s, T_PP, a1, b0, 0, 0); } break;
+        case 4: if (d_PP(A1, B1) < dh2) { if (m) emit(s, T_PPM, a1, a0, b1, b0); else emit(s, T_PP, a1, b1, 0, 0); } break;
+        case 5: if (d_PE(A1, B0, B1) < dh2) { if (m) emit(s, T_PEM, a1, a0, b0, b1); else emit(s, T_PE, a1, b0, b1, 0); } break;
+        case 6: if (d_PE(B0, A0, A1) < dh2) { if (m) emit(s, T_PEM, b0, b1, a0, a1); else emit(s, T_PE, b0, a0, a1, 0); } break;
+        case 7: if (d_PE(B1, A0, A1) < dh2) { if (m) emit(s, T_PEM, b1, b0, a0, a1); else emit(s, T_PE, b1, a0, a1, 0); } break;
+        default: if (d_EE(A0, A1, B0, B1) < dh2) { if (m) emit(s, T_EEM, a0, a1, b0, b1); else emit(s, T_EE, a0, a1, b0, b1); } break;
+    }
+}
+
+// one thread per boundary triangle; points hashed with mode 0
+__global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
+                                                 const double* __restrict__ x, double dh, double dh2, double inv_dx,
+                                                 const unsigned long long* __restrict__ uk, const int* __restrict__ us,
+                                                 const int* __restrict__ nu_p, const int* __restrict__ ids, RowSink sink) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbt) return;
+    const int nu = *nu_p;
+    const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
+    const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
+    const C3 lo = cell_of(vmin(vmin(A, B), C), inv_dx), hi = cell_of(vmax(vmax(A, B), C), inv_dx);
+    for (long long cx = lo.x; cx <= hi.x; ++cx)
+        for (long long cy = lo.y; cy <= hi.y; ++cy)
+            for (long long cz = lo.z; cz <= hi.z; ++cz) {
+                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                if (c < 0) continue;
+                for (int k = us[c]; k < us[c + 1]; ++k) {
+                    const int j = ids[k];
+                    const int p = bp[j];
+                    const C3 plo = cell_of(ld3(x, p) - mk(dh, dh, dh), inv_dx);
+                    const C3 first = cmax(lo, plo);
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    attempt_pt(x, dh, dh2, p, t0, t1, t2, sink);
+                }
+            }
+}
+
+// one thread per boundary edge (query, box +- dh); stored edges hashed with mode 1
+__global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
+                                                 const double* __restrict__ x0, double dh, double dh2, double inv_dx,
+                                                 const unsigned long long* __restrict__ uk, const int* __restrict__ us,
+                                                 const int* __restrict__ nu_p, const int* __restrict__ ids, RowSink sink) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbe) return;
+    const int nu = *nu_p;
+    const int a0 = be[2 * i], a1 = be[2 * i + 1];
+    const v3 A0 = ld3(x, a0), A1 = ld3(x, a1);
+    const v3 d = mk(dh, dh, dh);
+    const C3 lo = cell_of(vmin(A0, A1) - d, inv_dx), hi = cell_of(vmax(A0, A1) + d, inv_dx);
+    for (long long cx = lo.x; cx <= hi.x; ++cx)
+        for (long long cy = lo.y; cy <= hi.y; ++cy)
+            for (long long cz = lo.z; cz <= hi.z; ++cz) {
+                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                if (c < 0) continue;
+                for (int k = us[c]; k < us[c + 1]; ++k) {
+                    const int j = ids[k];
+                    if (!(i < j)) continue;
+                    const int b0 = be[2 * j], b1 = be[2 * j + 1];
+                    const C3 slo = cell_of(vmin(ld3(x, b0), ld3(x, b1)), inv_dx);
+                    const C3 first = cmax(lo, slo);
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    attempt_ee(x, x0, dh, dh2, a0, a1, b0, b1, sink);
+                }
+            }
+}
+
+// ---------------------------------------------------------------- CCD step filter
+__device__ __forceinline__ void atomic_min_pos(unsigned long long* slot, double v) {
+    if (v >= 0.0) atomicMin(slot, (unsigned long long)__double_as_longlong(v));
+}
+
+// compute_filter_3D_PT (NEWTON_IPC.py:377-406): triangles query their moving bbox
+__global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
+                                                const double* __restrict__ x, const double* __restrict__ p, double dh, double inv_dx,
+                                                double eta, const unsigned long long* __restrict__ uk, const int* __restrict__ us,
+                                                const int* __restrict__ nu_p, const int* __restrict__ ids,
+                                                unsigned long long* __restrict__ alpha) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbt) return;
+    const int nu = *nu_p;
+    const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
+    const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
+    const v3 dA = ld3(p, t0), dB = ld3(p, t1), dC = ld3(p, t2);
+    const v3 mn = vmin(vmin(vmin(A, A + dA), vmin(B, B + dB)), vmin(C, C + dC));
+    const v3 mx = vmax(vmax(vmax(A, A + dA), vmax(B, B + dB)), vmax(C, C + dC));
+    const C3 lo = cell_of(mn, inv_dx), hi = cell_of(mx, inv_dx);
+    const v3 d = mk(dh, dh, dh);
+    for (long long cx = lo.x; cx <= hi.x; ++cx)
+        for (long long cy = lo.y; cy <= hi.y; ++cy)
+            for (long long cz = lo.z; cz <= hi.z; ++cz) {
+                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                if (c < 0) continue;
+                for (int k = us[c]; k < us[c + 1]; ++k) {
+                    const int pp = bp[ids[k]];
+                    if (pp == t0 || pp == t1 || pp == t2) continue;
+                    const v3 P = ld3(x, pp), dP = ld3(p, pp);
+                    const C3 plo = cell_of(vmin(P, P + dP) - d, inv_dx);
+                    const C3 first = cmax(lo, plo);
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (!pt_aabb_moving(P, A, B, C, dP, dA, dB, dC, dh)) continue;
+                    const double d2 = pt_dist2(P, A, B, C);
+                    atomic_min_pos(alpha, pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, d2));
+                }
+            }
+}
+
+// compute_filter_3D_EE (NEWTON_IPC.py:409-440): edges query moving bbox +- dh
+__global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
+                                                const double* __restrict__ p, double dh, double inv_dx, double eta,
+                                                const unsigned long long* __restrict__ uk, const int* __restrict__ us,
+                                                const int* __restrict__ nu_p, const int* __restrict__ ids,
+                                                unsigned long long* __restrict__ alpha) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbe) return;
+    const int nu = *nu_p;
+    const int a0 = be[2 * i], a1 = be[2 * i + 1];
+    const v3 A0 = ld3(x, a0), A1 = ld3(x, a1), dA0 = ld3(p, a0), dA1 = ld3(p, a1);
+    const v3 d = mk(dh, dh, dh);
+    const v3 mn = vmin(vmin(A0, A0 + dA0), vmin(A1, A1 + dA1)), mx = vmax(vmax(A0, A0 + dA0), vmax(A1, A1 + dA1));
+    const C3 lo = cell_of(mn - d, inv_dx), hi = cell_of(mx + d, inv_dx);
+    for (long long cx = lo.x; cx <= hi.x; ++cx)
+        for (long long cy = lo.y; cy <= hi.y; ++cy)
+            for (long long cz = lo.z; cz <= hi.z; ++cz) {
+                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                if (c < 0) continue;
+                for (int k = us[c]; k < us[c + 1]; ++k) {
+                    const int j = ids[k];
+                    if (!(i < j)) continue;
+                    const int b0 = be[2 * j], b1 = be[2 * j + 1];
+                    if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) continue;
+                    const v3 B0 = ld3(x, b0), B1 = ld3(x, b1), dB0 = ld3(p, b0), dB1 = ld3(p, b1);
+                    const C3 slo = cell_of(vmin(vmin(B0, B0 + dB0), vmin(B1, B1 + dB1)), inv_dx);
+                    const C3 first = cmax(lo, slo);
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (!ee_aabb_moving(A0, A1, B0, B1, dA0, dA1, dB0, dB1, dh)) continue;
+                    const double d2 = ee_dist2(A0, A1, B0, B1);
+                    atomic_min_pos(alpha, ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2));
+                }
+            }
+}
+
+// compute_filter_3D_inversion_free (NEWTON_IPC.py:443-453)
+__global__ void __launch_bounds__(128) k_ccd_inversion(int nT, const int4* __restrict__ tets, const double* __restrict__ x,
+                                                       const double* __restrict__ p, double eta, unsigned long long* __restrict__ alpha) {
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= nT) return;
+    const int4 t = tets[e];
+    const v3 X[4] = {ld3(x, t.x), ld3(x, t.y), ld3(x, t.z), ld3(x, t.w)};
+    const v3 P[4] = {ld3(p, t.x), ld3(p, t.y), ld3(p, t.z), ld3(p, t.w)};
+    atomic_min_pos(alpha, inversion_free_step(X, P, eta));
+}
+
+// check_collision_3d (NEWTON_IPC.py:855-880): triangles query bbox cells, edges hashed +- dh
+__global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restrict__ bt, const int* __restrict__ be,
+                                                   const double* __restrict__ x, double dh, double inv_dx,
+                                                   const unsigned long long* __restrict__ uk, const int* __restrict__ us,
+                                                   const int* __restrict__ nu_p, const int* __restrict__ ids, int* __restrict__ hit) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nbt) return;
+    const int nu = *nu_p;
+    const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
+    const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
+    const C3 lo = cell_of(vmin(vmin(A, B), C), inv_dx), hi = cell_of(vmax(vmax(A, B), C), inv_dx);
+    const v3 d = mk(dh, dh, dh);
+    for (long long cx = lo.x; cx <= hi.x; ++cx)
+        for (long long cy = lo.y; cy <= hi.y; ++cy)
+            for (long long cz = lo.z; cz <= hi.z; ++cz) {
+                if (*(volatile int*)hit) return;
+                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                if (c < 0) continue;
+                for (int k = us[c]; k < us[c + 1]; ++k) {
+                    const int j = ids[k];
+                    const int a0 = be[2 * j], a1 = be[2 * j + 1];
+                    if (a0 == t0 || a0 == t1 || a0 == t2 || a1 == t0 || a1 == t1 || a1 == t2) continue;
+                    const v3 P = ld3(x, a0), Q = ld3(x, a1);
+                    const C3 slo = cell_of(vmin(P, Q) - d, inv_dx);
+                    const C3 first = cmax(lo, slo);
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (seg_tri(P, Q, A, B, C)) {
+                        atomicOr(hit, 1);
+                        return;
+                    }
+                }
+            }
+}
+
+// ---------------------------------------------------------------- row canonicalisation
+// width-2 / width-3 rows: one 63-bit key; width-4 rows: LSD two-pass (last index, then the
+// first three) with the stable radix sort.  21 bits per vertex index (< 2^21 vertices).
+__global__ void k_row_keys(int n, int width, int pass, const int4* __restrict__ rows, const int* __restrict__ perm,
+                           unsigned long long* __restrict__ keys, int* __restrict__ idx) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int src = perm ? perm[i] : i;
+    const int4 r = rows[src];
+    unsigned long long k;
+    if (width == 2) k = ((unsigned long long)r.x << 21) | (unsigned long long)r.y;
+    else if (width == 3 || pass == 1) k = ((unsigned long long)r.x << 42) | ((unsigned long long)r.y << 21) | (unsigned long long)r.z;
+    else k = (unsigned long long)r.w;
+    keys[i] = k;
+    idx[i] = src;
+}
+__global__ void k_row_gather_flag(int n, const int4* __restrict__ rows, const int* __restrict__ perm, int4* __restrict__ out,
+                                  int* __restrict__ flag) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int4 r = rows[perm[i]];
+    out[i] = r;
+    int f = 1;
+    if (i > 0) {
+        const int4 q = rows[perm[i - 1]];
+        f = !(q.x == r.x && q.y == r.y && q.z == r.z && q.w == r.w);
+    }
+    flag[i] = f;
+}
+__global__ void k_row_compact(int n, const int4* __restrict__ in, const int* __restrict__ flag, const int* __restrict__ pos,
+                              int4* __restrict__ out, int* __restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (flag[i]) out[pos[i]] = in[i];
+    if (i == n - 1) *count = pos[i] + flag[i];
+}
+
+// ---------------------------------------------------------------- host side
+static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+template <class F>
+static int cub_call(fipc_ctx* c, F&& f) {
+    size_t need = 0;
+    if (f(nullptr, need) != cudaSuccess) return FIPC_ERR_CUDA;
+    if (c->cub_tmp.ensure(need)) return FIPC_ERR_CUDA;
+    size_t have = c->cub_tmp.bytes;
+    if (f(c->cub_tmp.p, have) != cudaSuccess) return FIPC_ERR_CUDA;
+    return FIPC_OK;
+}
+
+// build grid g over n stored primitives; scal: device int scratch (overflow flag at [0])
+int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const double* x, const double* p, cudaStream_t s) {
+    g.n_entries = 0;
+    g.n_unique = 0;
+    if (g.counts.ensure(sizeof(long long) * (n + 1)) || g.offsets.ensure(sizeof(long long) * (n + 1)) ||
+        g.ncells.ensure(sizeof(int) * 2))
+        return FIPC_ERR_CUDA;
+    FIPC_CUDA(cudaMemsetAsync(g.ncells.p, 0, sizeof(int) * 2, s));
+    if (n == 0) return FIPC_OK;
+    int* ovf = g.ncells.as<int>() + 1;
+    k_cell_count<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, c->inv_dx, g.counts.as<long long>(), ovf);
+    FIPC_LAUNCHED();
+    long long* cnt = g.counts.as<long long>();
+    long long* off = g.offsets.as<long long>();
+    int st = cub_call(c, [&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, cnt, off, n, s); });
+    if (st) return st;
+    long long last_off = 0, last_cnt = 0;
+    int h_ovf = 0;
+    FIPC_CUDA(cudaMemcpyAsync(&last_off, off + n - 1, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    FIPC_CUDA(cudaMemcpyAsync(&last_cnt, cnt + n - 1, sizeof(long long), cudaMemcpyDeviceToHost, s));
+    FIPC_CUDA(cudaMemcpyAsync(&h_ovf, ovf, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FIPC_CUDA(cudaStreamSynchronize(s));
+    if (h_ovf) return FIPC_ERR_CAPACITY;
+    const long long total = last_off + last_cnt;
+    if (total > (1ll << 30)) return FIPC_ERR_CAPACITY;
+    g.n_entries = (int)total;
+    if (total == 0) return FIPC_OK;
+    if (g.keys.ensure(8 * total) || g.keys_alt.ensure(8 * total) || g.ids.ensure(4 * total) || g.ids_alt.ensure(4 * total) ||
+        g.ukeys.ensure(8 * total) || g.ustart.ensure(4 * (total + 1)) || g.tmp.ensure(4 * (total + 1)))
+        return FIPC_ERR_CUDA;
+    k_cell_emit<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, c->inv_dx, off, cnt, g.keys.as<unsigned long long>(),
+                                             g.ids.as<int>());
+    FIPC_LAUNCHED();
+    cub::DoubleBuffer<unsigned long long> kb(g.keys.as<unsigned long long>(), g.keys_alt.as<unsigned long long>());
+    cub::DoubleBuffer<int> vb(g.ids.as<int>(), g.ids_alt.as<int>());
+    const int N = (int)total;
+    st = cub_call(c, [&](void* t, size_t& b) { return cub::DeviceRadixSort::SortPairs(t, b, kb, vb, N, 0, 63, s); });
+    if (st) return st;
+    if (kb.Current() != g.keys.as<unsigned long long>()) {
+        FIPC_CUDA(cudaMemcpyAsync(g.keys.p, kb.Current(), 8 * total, cudaMemcpyDeviceToDevice, s));
+        FIPC_CUDA(cudaMemcpyAsync(g.ids.p, vb.Current(), 4 * total, cudaMemcpyDeviceToDevice, s));
+    }
+    int* runs = g.tmp.as<int>();   // run lengths
+    int* nu = g.ncells.as<int>();
+    st = cub_call(c, [&](void* t, size_t& b) {
+        return cub::DeviceRunLengthEncode::Encode(t, b, g.keys.as<unsigned long long>(), g.ukeys.as<unsigned long long>(), runs, nu,
+                                                  N, s);
+    });
+    if (st) return st;
+    st = cub_call(c, [&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, runs, g.ustart.as<int>(), N + 1, s); });
+    if (st) return st;
+    return FIPC_OK;
+}
+
+// sort + unique each list in place (rows_tmp as staging); returns counts in c->h_counts
+static int canonicalize_rows(fipc_ctx* c, cudaStream_t s) {
+    int h[N_TYPES + 1];
+    FIPC_CUDA(cudaMemcpyAsync(h, c->d_counts, sizeof(int) * (N_TYPES + 1), cudaMemcpyDeviceToHost, s));
+    FIPC_CUDA(cudaStreamSynchronize(s));
+    if (h[N_TYPES]) return FIPC_ERR_CAPACITY;
+    static const int width[N_TYPES] = {2, 3, 4, 4, 4, 4, 4};
+    for (int t = 0; t < N_TYPES; ++t) {
+        const int n = h[t];
+        c->h_counts[t] = n;
+        if (n <= 1) continue;
+        if (c->rows_tmp.ensure(16ll * n) || c->sort_keys.ensure(8ll * n) || c->sort_keys_alt.ensure(8ll * n) ||
+            c->sort_vals.ensure(4ll * n) || c->sort_vals_alt.ensure(4ll * n) || c->flags.ensure(4ll * n) || c->scan.ensure(4ll * n))
+            return FIPC_ERR_CUDA;
+        int4* rows = c->rows[t].as<int4>();
+        const int* perm = nullptr;
+        const int passes = width[t] == 4 ? 2 : 1;
+        for (int pass = 0; pass < passes; ++pass) {
+            const int kpass = width[t] == 4 ? pass : 1;
+            k_row_keys<<<nblk(n, 256), 256, 0, s>>>(n, width[t], kpass, rows, perm, c->sort_keys.as<unsigned long long>(),
+                                                   c->sort_vals.as<int>());
+            FIPC_LAUNCHED();
+            cub::DoubleBuffer<unsigned long long> kb(c->sort_keys.as<unsigned long long>(), c->sort_keys_alt.as<unsigned long long>());
+            cub::DoubleBuffer<int> vb(c->sort_vals.as<int>(), c->sort_vals_alt.as<int>());
+            const int end_bit = (width[t] == 2) ? 42 : ((kpass == 1) ? 63 : 32);
+            int st = cub_call(c, [&](void* tm, size_t& b) { return cub::DeviceRadixSort::SortPairs(tm, b, kb, vb, n, 0, end_bit, s); });
+            if (st) return st;
+            if (vb.Current() != c->sort_vals.as<int>())
+                FIPC_CUDA(cudaMemcpyAsync(c->sort_vals.p, vb.Current(), 4ll * n, cudaMemcpyDeviceToDevice, s));
+            // the permutation for the next pass lives in sort_vals_alt
+            FIPC_CUDA(cudaMemcpyAsync(c->sort_vals_alt.p, c->sort_vals.p, 4ll * n, cudaMemcpyDeviceToDevice, s));
+            perm = c->sort_vals_alt.as<int>();
+        }
+        k_row_gather_flag<<<nblk(n, 256), 256, 0, s>>>(n, rows, perm, c->rows_tmp.as<int4>(), c->flags.as<int>());
+        FIPC_LAUNCHED();
+        int* flg = c->flags.as<int>();
+        int* pos = c->scan.as<int>();
+        int st = cub_call(c, [&](void* tm, size_t& b) { return cub::DeviceScan::ExclusiveSum(tm, b, flg, pos, n, s); });
+        if (st) return st;
+        k_row_compact<<<nblk(n, 256), 256, 0, s>>>(n, c->rows_tmp.as<int4>(), flg, pos, rows, c->d_counts + t);
+        FIPC_LAUNCHED();
+    }
+    FIPC_CUDA(cudaMemcpyAsync(h, c->d_counts, sizeof(int) * N_TYPES, cudaMemcpyDeviceToHost, s));
+    FIPC_CUDA(cudaStreamSynchronize(s));
+    for (int t = 0; t < N_TYPES; ++t) c->h_counts[t] = h[t];
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+
+int ensure_row_capacity(fipc_ctx* c, int cap) {
+    if (cap <= c->cap) return FIPC_OK;
+    for (int t = 0; t < N_TYPES; ++t)
+        if (c->rows[t].ensure(16ll * cap)) return FIPC_ERR_CUDA;
+    c->cap = cap;
+    return FIPC_OK;
+}
+
+// find_constraints (NEWTON_IPC.py:337-357) into c->rows / c->h_counts
+int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        FIPC_CUDA(cudaMemsetAsync(c->d_counts, 0, sizeof(int) * (N_TYPES + 1), s));
+        RowSink sink;
+        for (int t = 0; t < N_TYPES; ++t) sink.rows[t] = c->rows[t].as<int4>();
+        sink.counts = c->d_counts;
+        sink.cap = c->cap;
+        int st = build_grid(c, c->gp, 0, c->nBP, c->bp, x, nullptr, s);
+        if (st) return st;
+        if (c->gp.n_entries > 0 && c->nBT > 0) {
+            k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, c->inv_dx,
+                                                         c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
+                                                         c->gp.ncells.as<int>(), c->gp.ids.as<int>(), sink);
+            FIPC_LAUNCHED();
+        }
+        st = build_grid(c, c->ge, 1, c->nBE, c->be, x, nullptr, s);
+        if (st) return st;
+        if (c->ge.n_entries > 0) {
+            k_find_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, c->inv_dx,
+                                                         c->ge.ukeys.as<unsigned long long>(), c->ge.ustart.as<int>(),
+                                                         c->ge.ncells.as<int>(), c->ge.ids.as<int>(), sink);
+            FIPC_LAUNCHED();
+        }
+        FIPC_CUDA(cudaGetLastError());
+        st = canonicalize_rows(c, s);
+        if (st == FIPC_ERR_CAPACITY) {
+            int h[N_TYPES];
+            FIPC_CUDA(cudaMemcpy(h, c->d_counts, sizeof(int) * N_TYPES, cudaMemcpyDeviceToHost));
+            int need = c->cap;
+            for (int t = 0; t < N_TYPES; ++t) need = h[t] > need ? h[t] : need;
+            if (ensure_row_capacity(c, 2 * need)) return FIPC_ERR_CUDA;
+            continue;
+        }
+        return st;
+    }
+    return FIPC_ERR_CAPACITY;
+}
+
+// compute_intersection_free_step_size (NEWTON_IPC.py:456-468); result in *alpha_h
+int ccd_step(fipc_ctx* c, const double* x, const double* p, double eta, bool inversion, double* alpha_h, cudaStream_t s) {
+    if (c->scal.ensure(64)) return FIPC_ERR_CUDA;
+    unsigned long long* slot = c->scal.as<unsigned long long>();
+    const double one = 1.0;
+    FIPC_CUDA(cudaMemcpyAsync(slot, &one, 8, cudaMemcpyHostToDevice, s));
+    int st = build_grid(c, c->gp, 2, c->nBP, c->bp, x, p, s);
+    if (st) return st;
+    if (c->gp.n_entries > 0 && c->nBT > 0) {
+        k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, c->inv_dx, eta,
+                                                    c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
+                                                    c->gp.ncells.as<int>(), c->gp.ids.as<int>(), slot);
+        FIPC_LAUNCHED();
+    }
+    st = build_grid(c, c->ge, 3, c->nBE, c->be, x, p, s);
+    if (st) return st;
+    if (c->ge.n_entries > 0) {
+        k_ccd_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, c->inv_dx, eta, c->ge.ukeys.as<unsigned long long>(),
+                                                    c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), slot);
+        FIPC_LAUNCHED();
+    }
+    if (inversion && c->nT > 0) {
+        k_ccd_inversion<<<nblk(c->nT, 128), 128, 0, s>>>(c->nT, (const int4*)c->tets, x, p, eta, slot);
+        FIPC_LAUNCHED();
+    }
+    FIPC_CUDA(cudaGetLastError());
+    FIPC_CUDA(cudaMemcpyAsync(alpha_h, slot, 8, cudaMemcpyDeviceToHost, s));
+    FIPC_CUDA(cudaStreamSynchronize(s));
+    return FIPC_OK;
+}
+
+int check_collision(fipc_ctx* c, const double* x, int* hit_h, cudaStream_t s) {
+    if (c->scal.ensure(64)) return FIPC_ERR_CUDA;
+    int* hit = (int*)(c->scal.as<char>() + 16);
+    FIPC_CUDA(cudaMemsetAsync(hit, 0, sizeof(int), s));
+    int st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, s);
+    if (st) return st;
+    if (c->ge.n_entries > 0 && c->nBT > 0) {
+        k_collision<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, c->inv_dx, c->ge.ukeys.as<unsigned long long>(),
+                                                       c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), hit);
+        FIPC_LAUNCHED();
+    }
+    FIPC_CUDA(cudaGetLastError());
+    FIPC_CUDA(cudaMemcpyAsync(hit_h, hit, sizeof(int), cudaMemcpyDeviceToHost, s));
+    FIPC_CUDA(cudaStreamSynchronize(s));
+    return FIPC_OK;
+}
+
+}  // namespace fipc

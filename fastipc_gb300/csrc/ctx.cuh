@@ -1,0 +1,108 @@
+// Scene context shared by the translation units of libfastipc.so: the device-resident state
+// that projects/FastIPC/NEWTON_IPC.py keeps in module-global Taichi fields (mesh, rest shape,
+// mass, constraint lists, the assembled system, scratch), plus device-buffer bookkeeping.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include <atomic>
+
+#include "common.cuh"
+
+namespace fipc {
+
+// number of kernels this library launched (reported by fipc_launch_count)
+extern std::atomic<long long> g_launches;
+
+#define FIPC_CUDA(call)                                  \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return FIPC_ERR_CUDA;     \
+    } while (0)
+
+#define FIPC_LAUNCHED() (g_launches.fetch_add(1, std::memory_order_relaxed))
+
+// Grow-only device buffer.  Contents are not preserved across growth.
+struct DBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t need) {
+        if (need <= bytes) return FIPC_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        size_t nb = need + need / 4 + 256;
+        if (cudaMalloc(&p, nb) != cudaSuccess) {
+            bytes = 0;
+            return FIPC_ERR_CUDA;
+        }
+        bytes = nb;
+        return FIPC_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    template <class T>
+    T* as() const { return (T*)p; }
+};
+
+// sorted spatial-hash grid over primitives: (cell key, primitive id) pairs sorted by key,
+// unique keys and the start of each key's run
+struct Grid {
+    DBuf keys, ids, keys_alt, ids_alt, ukeys, ustart, counts, offsets, ncells, tmp;
+    int n_entries = 0, n_unique = 0;
+};
+
+struct fipc_ctx_impl {
+    int nV = 0, nT = 0, nBP = 0, nBE = 0, nBT = 0;
+    // mesh (device)
+    int *tets = nullptr, *bp = nullptr, *be = nullptr, *bt = nullptr;
+    double *dminv = nullptr, *vol = nullptr, *lam = nullptr, *mu = nullptr, *mass = nullptr, *x0 = nullptr;
+    double dhat2 = 0, dhat = 0, kappa = 0, inv_dx = 0, dt = 0;
+    // static elastic + inertia BSR pattern (full, both triangles)
+    int nnzb = 0, n_upper = 0;
+    int *row_ptr = nullptr, *col_idx = nullptr;
+    int *up_pos = nullptr, *up_tpos = nullptr, *up_row = nullptr, *up_cptr = nullptr, *up_contrib = nullptr;
+    int *vt_ptr = nullptr, *vt_list = nullptr;   // vertex -> (tet*4 + local) for the gradient gather
+    int* diag_pos = nullptr;                     // BSR position of each vertex's diagonal block
+    // per-iteration element data and the system
+    double *elem_g = nullptr, *elem_H = nullptr, *bsr_val = nullptr, *rhs = nullptr;
+    // constraint lists (capacity rows of 4 ints each) and counts
+    DBuf rows[N_TYPES], rows_tmp, sort_keys, sort_keys_alt, sort_vals, sort_vals_alt, flags, scan, cub_tmp;
+    int *d_counts = nullptr;     // [N_TYPES + 1] device (last: overflow flag)
+    int h_counts[N_TYPES] = {0};
+    int cap = 0;
+    // contact system
+    DBuf c_g, c_H, c_keys, c_keys_alt, c_vals, c_vals_alt, c_ukeys, c_ucount, c_ustart, c_val, c_rowptr, c_col;
+    int c_rows = 0, c_nnzb = 0;
+    // PCG
+    DBuf pcg_vec, pcg_part;
+    // grids
+    Grid gp, ge;
+    // small device scalars: [0] alpha bits, [1] hit flag, reductions ...
+    DBuf scal, red;
+};
+
+// ---------------------------------------------------------------- shared device helpers
+#if defined(__CUDACC__)
+__device__ __forceinline__ v3 ld3(const double* __restrict__ x, int i) {
+    return v3{__ldg(x + 3 * i), __ldg(x + 3 * i + 1), __ldg(x + 3 * i + 2)};
+}
+#endif
+
+constexpr int RED_BLOCKS = 304;     // 2 x 152 SMs: fixed reduction grid (deterministic sums)
+constexpr int RED_THREADS = 256;
+
+// cell key of integer cell coordinates (21 bits per axis, offset 2^20)
+FIPC_HD unsigned long long cell_key(long long i, long long j, long long k) {
+    const long long off = 1ll << 20;
+    auto c = [](long long v) { return v < 0 ? 0ll : (v > (1ll << 21) - 1 ? (1ll << 21) - 1 : v); };
+    return ((unsigned long long)c(i + off) << 42) | ((unsigned long long)c(j + off) << 21) | (unsigned long long)c(k + off);
+}
+
+}  // namespace fipc
+
+using fipc_ctx = fipc::fipc_ctx_impl;

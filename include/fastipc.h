@@ -1,0 +1,118 @@
+/*
+ * libfastipc — C ABI of the GB300 (sm_103a) implementation of FastIPC's IPC Newton inner loop.
+ *
+ * Each entry point replaces one Taichi kernel (or one piece of the native a.so) of the
+ * reference, cited as file:line relative to the FastIPC checkout.  All array arguments are
+ * DEVICE pointers unless the name ends in _h (host).  Positions are vertex-major [V][3] FP64;
+ * constraint rows are [n][4] int32 (unused trailing ids zero); tets [T][4] int32.  `stream`
+ * is a cudaStream_t (NULL for the legacy default stream).  Every function returns a status:
+ * 0 ok, 1 capacity exceeded, 2 iteration limit, 3 non-finite value, 4 CUDA error,
+ * 5 invalid argument.  The library allocates its own scratch inside a context and never
+ * frees caller memory.  Calls on one context are not reentrant.
+ */
+#ifndef FASTIPC_H
+#define FASTIPC_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct fipc_ctx_impl fipc_ctx;
+
+/* constraint list ids, in the reference's list order (NEWTON_IPC.py:349) */
+enum { FIPC_PP = 0, FIPC_PE = 1, FIPC_PT = 2, FIPC_EE = 3, FIPC_EEM = 4, FIPC_PPM = 5, FIPC_PEM = 6 };
+
+/* ---- stateless element kernels ------------------------------------------------------------ */
+
+/* Neo-Hookean tets: gradient g [T][12] and the 10 upper 3x3 blocks Hu [T][90]
+ * ((0,0)(0,1)(0,2)(0,3)(1,1)(1,2)(1,3)(2,2)(2,3)(3,3)) of dt^2 vol0 psi(Ds Dm^-1), energy E [T]
+ * (may be NULL).  Replaces compute_elasticity, NEWTON_IPC.py:568-691, with the material of
+ * common/physics/neo_hookean.py:6-131. */
+int fipc_elasticity(int n_tets, const int* tets, const double* x, const double* dm_inv, const double* vol,
+                    const double* lam, const double* mu, double dt, double* E, double* g, double* Hu, void* stream);
+
+/* Barrier energy E [n], gradient g [n][12] and PSD-projected Hessian H [n][16][9] (3x3 vertex
+ * blocks v*4+w) of n rows of one constraint list; x0 = rest positions (mollified lists).
+ * Replaces PP/PE/PT/EE/EEM/PPM/PEM_g_and_H, common/math/ipc.py:67-329, and the a.so
+ * project_pd_{6,9,12} calls of common/math/math_tools.py:101-128. */
+int fipc_barrier_rows(int type, int n_rows, const int* rows, const double* x, const double* x0, double dhat2,
+                      double kappa, double* E, double* g, double* H, void* stream);
+
+/* Time of impact of explicit primitive pairs xq/pq [n][4][3] (kind 0: point-triangle,
+ * 1: edge-edge) with the current-distance argument computed as NEWTON_IPC.py:404/:438 do.
+ * Replaces a.so point_triangle_ccd / edge_edge_ccd (common/math/wrapper/wrapper.cpp:254-328). */
+int fipc_ccd_pairs(int kind, int n, const double* xq, const double* pq, double eta, double* toc, void* stream);
+
+/* Inversion-free step per tet, xs/ps [n][4][3].  Replaces
+ * get_smallest_positive_real_cubic_root, common/math/math_tools.py:161-181. */
+int fipc_inversion_free_pairs(int n, const double* xs, const double* ps, double eta, double* out, void* stream);
+
+/* ---- vector updates of the Newton loop ---------------------------------------------------- */
+int fipc_compute_xn_and_xtilde(int n_verts, const double* x, const double* v, double dt, double gravity, double* xn,
+                               double* xtilde, void* stream);                 /* NEWTON_IPC.py:497-502 */
+int fipc_move_nodes(int n_verts, const unsigned char* fixed, const double* target, double* x, double* xtilde,
+                    void* stream);                                             /* NEWTON_IPC.py:505-511 */
+int fipc_apply_sol(int n_verts, const double* xprev, const double* sol, double alpha, double* x,
+                   void* stream);                                              /* NEWTON_IPC.py:792-796 */
+int fipc_compute_v(int n_verts, const double* x, const double* xn, double dt, double* v,
+                   void* stream);                                              /* NEWTON_IPC.py:799-802 */
+
+/* ---- scene context: the module state of NEWTON_IPC.py -------------------------------------- */
+
+/* Host inputs.  Computes rest shapes, volumes and lumped mass (NEWTON_IPC.py:485-494), the
+ * adaptive kappa x10 (:116-124, :943), the hash cell 1/mean boundary edge (:127-134, :944)
+ * and the static block pattern.  x_rest is also the mollifier rest shape (save_x0, :780-783). */
+int fipc_ctx_create(fipc_ctx** ctx, int n_verts, int n_tets, const int* tets_h, const double* x_rest_h,
+                    const double* lam_h, const double* mu_h, double rho, int n_bp, const int* bp_h, int n_be,
+                    const int* be_h, int n_bt, const int* bt_h, double dhat2, double dt);
+int fipc_ctx_destroy(fipc_ctx* ctx);
+int fipc_ctx_params(fipc_ctx* ctx, double* kappa_h, double* inv_dx_h, int* nnzb_h);
+int fipc_ctx_set_params(fipc_ctx* ctx, double kappa, double inv_dx);
+int fipc_ctx_mass(fipc_ctx* ctx, double* mass_h);
+int fipc_ctx_set_x0(fipc_ctx* ctx, const double* x0, void* stream);
+
+/* find_constraints, NEWTON_IPC.py:337-357 (spatial hash :213-334, dedup :348-356): the seven
+ * lists, sorted lexicographically and de-duplicated; counts_h [7] receives their sizes. */
+int fipc_find_constraints(fipc_ctx* ctx, const double* x, int* counts_h, void* stream);
+int fipc_get_constraints(fipc_ctx* ctx, int type, int* rows, void* stream);
+
+/* compute_hessian_and_gradient, NEWTON_IPC.py:736-747 (inertia :558-567, elasticity
+ * :568-691, barriers :692-733): block-sparse system and right-hand side -grad. */
+int fipc_compute_hessian_and_gradient(fipc_ctx* ctx, const double* x, const double* xtilde, void* stream);
+int fipc_system_sizes(fipc_ctx* ctx, int* nnzb_elastic_h, int* nnzb_contact_h);
+int fipc_export_system(fipc_ctx* ctx, int* row_ptr, int* col_idx, double* val, int* c_row_ptr, int* c_col_idx,
+                       double* c_val, double* rhs, void* stream);
+
+/* solve_system, NEWTON_IPC.py:750-777: Newton direction with Dirichlet vertices (fixed [V])
+ * held at zero, by block-Jacobi PCG to relative residual rtol (iters_h: iterations used). */
+int fipc_solve_system(fipc_ctx* ctx, const unsigned char* fixed, double rtol, int maxit, double* sol, int* iters_h,
+                      void* stream);
+
+/* output_residual, NEWTON_IPC.py:805-812: max |sol| */
+int fipc_output_residual(fipc_ctx* ctx, const double* sol, double* res_h, void* stream);
+
+/* compute_energy, NEWTON_IPC.py:514-542, over the lists of the last find_constraints */
+int fipc_compute_energy(fipc_ctx* ctx, const double* x, const double* xtilde, double* e_h, void* stream);
+
+/* compute_intersection_free_step_size, NEWTON_IPC.py:456-468 (PT :377-406, EE :409-440,
+ * inversion :443-453 when `inversion` is nonzero) */
+int fipc_compute_intersection_free_step_size(fipc_ctx* ctx, const double* x, const double* p, double eta, int inversion,
+                                             double* alpha_h, void* stream);
+
+/* check_collision, NEWTON_IPC.py:855-886 */
+int fipc_check_collision(fipc_ctx* ctx, const double* x, int* hit_h, void* stream);
+
+/* ---- diagnostics -------------------------------------------------------------------------- */
+/* Time every launch of one kernel with CUDA events on its stream (1 PCG SpMV, 2 PCG update,
+ * 3 Neo-Hookean element, 4 barrier rows, 5 elastic assembly; 0 off) and read back the summed
+ * milliseconds, launch count and the launches' algorithmic bytes and flops. */
+int fipc_profile_enable(int kernel_id);
+int fipc_profile_read(double* total_ms_h, long long* launches_h, double* bytes_h, double* flops_h);
+long long fipc_launch_count(void);           /* kernels launched by this library so far */
+const char* fipc_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

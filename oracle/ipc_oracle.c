@@ -1380,3 +1380,98 @@ int oracle_num_threads(void) {
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------------------------
+ * block-sparse (3x3) assembly and PCG for large scenes (the timed CPU baseline)
+ * ---------------------------------------------------------------------------------------- */
+/* val[pos16[e*16 + a*4 + b]] += block (a, b) of the element Hessian H[e] (12x12 row-major) */
+void oracle_bsr_accumulate(int T, const long long* pos16, const double* H, double* val) {
+    for (int e = 0; e < T; ++e)
+        for (int a = 0; a < 4; ++a)
+            for (int b = 0; b < 4; ++b) {
+                double* dst = val + 9 * pos16[16 * (long long)e + a * 4 + b];
+                const double* src = H + 144 * (long long)e;
+                for (int i = 0; i < 3; ++i)
+                    for (int j = 0; j < 3; ++j) dst[i * 3 + j] += src[(3 * a + i) * 12 + 3 * b + j];
+            }
+}
+
+/* y = A p over the rows of a 3x3 block-sparse matrix (rows of fixed vertices are zero) */
+static void bsr_spmv(int nV, const long long* rp, const int* ci, const double* va, const unsigned char* fixed, const double* p,
+                     double* y, int accumulate) {
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < nV; ++i) {
+        double s0 = 0, s1 = 0, s2 = 0;
+        if (!fixed[i])
+            for (long long k = rp[i]; k < rp[i + 1]; ++k) {
+                const int j = ci[k];
+                if (fixed[j]) continue;
+                const double* B = va + 9 * k;
+                s0 += B[0] * p[3 * j] + B[1] * p[3 * j + 1] + B[2] * p[3 * j + 2];
+                s1 += B[3] * p[3 * j] + B[4] * p[3 * j + 1] + B[5] * p[3 * j + 2];
+                s2 += B[6] * p[3 * j] + B[7] * p[3 * j + 1] + B[8] * p[3 * j + 2];
+            }
+        if (accumulate) { y[3 * i] += s0; y[3 * i + 1] += s1; y[3 * i + 2] += s2; }
+        else { y[3 * i] = s0; y[3 * i + 1] = s1; y[3 * i + 2] = s2; }
+    }
+}
+
+static double pdot(long long n, const double* a, const double* b) {
+    double s = 0;
+    #pragma omp parallel for reduction(+ : s) schedule(static)
+    for (long long i = 0; i < n; ++i) s += a[i] * b[i];
+    return s;
+}
+
+/* block-Jacobi PCG on elastic (rp, ci, va) + contact (crp, cci, cva) block-sparse matrices;
+ * diag_pos: position of each diagonal block in the elastic matrix.  Returns iterations. */
+int oracle_bsr_pcg(int nV, const long long* rp, const int* ci, const double* va, const long long* crp, const int* cci,
+                   const double* cva, const long long* diag_pos, const double* b, const unsigned char* fixed, double rtol, int maxit,
+                   double* x) {
+    const long long n = 3ll * nV;
+    double *r = malloc(8 * n), *z = malloc(8 * n), *p = malloc(8 * n), *Ap = malloc(8 * n), *Mi = malloc(72 * (long long)nV);
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < nV; ++i) {
+        double B[9];
+        if (fixed[i]) { for (int k = 0; k < 9; ++k) B[k] = (k % 4 == 0); }
+        else {
+            for (int k = 0; k < 9; ++k) B[k] = va[9 * diag_pos[i] + k];
+            for (long long k = crp[i]; k < crp[i + 1]; ++k)
+                if (cci[k] == i) for (int q = 0; q < 9; ++q) B[q] += cva[9 * k + q];
+        }
+        inv3(B, Mi + 9 * i);
+    }
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < nV; ++i)
+        for (int d = 0; d < 3; ++d) {
+            x[3 * i + d] = 0;
+            r[3 * i + d] = fixed[i] ? 0 : b[3 * i + d];
+        }
+    #pragma omp parallel for schedule(static)
+    for (int i = 0; i < nV; ++i)
+        for (int d = 0; d < 3; ++d) {
+            z[3 * i + d] = Mi[9 * i + 3 * d] * r[3 * i] + Mi[9 * i + 3 * d + 1] * r[3 * i + 1] + Mi[9 * i + 3 * d + 2] * r[3 * i + 2];
+            p[3 * i + d] = z[3 * i + d];
+        }
+    double rz = pdot(n, r, z), rr0 = pdot(n, r, r);
+    int it = 0;
+    for (; it < maxit; ++it) {
+        const double rr = pdot(n, r, r);
+        if (rr <= rtol * rtol * rr0 || rr0 == 0) break;
+        bsr_spmv(nV, rp, ci, va, fixed, p, Ap, 0);
+        bsr_spmv(nV, crp, cci, cva, fixed, p, Ap, 1);
+        const double alpha = rz / pdot(n, p, Ap);
+        #pragma omp parallel for schedule(static)
+        for (long long i = 0; i < n; ++i) { x[i] += alpha * p[i]; r[i] -= alpha * Ap[i]; }
+        #pragma omp parallel for schedule(static)
+        for (int i = 0; i < nV; ++i)
+            for (int d = 0; d < 3; ++d)
+                z[3 * i + d] = Mi[9 * i + 3 * d] * r[3 * i] + Mi[9 * i + 3 * d + 1] * r[3 * i + 1] + Mi[9 * i + 3 * d + 2] * r[3 * i + 2];
+        const double rz2 = pdot(n, r, z), beta = rz2 / rz;
+        rz = rz2;
+        #pragma omp parallel for schedule(static)
+        for (long long i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
+    }
+    free(r); free(z); free(p); free(Ap); free(Mi);
+    return it;
+}

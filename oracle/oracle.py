@@ -200,6 +200,8 @@ class OracleSim:
         self.rows = [np.zeros((0, w), np.int32) for w in TYPE_NV]
         self.newton_iters = []
         self.pcg_iters = []
+        if solver == 'bsr':
+            self._bsr_pattern()
 
     # NEWTON_IPC.py:485-494, 145-155
     def compute_restT_and_m(self):
@@ -276,8 +278,60 @@ class OracleSim:
                                    _p(self.Dm), _p(self.la), _p(self.mu), D(self.dt), _p(self.x0), _p(counts, np.int32),
                                    _p(allr, np.int32), D(self.dhat2), D(self.kappa))
 
+    # static 3x3 block pattern of inertia + elasticity (large scenes: solver='bsr')
+    def _bsr_pattern(self):
+        nV, t = len(self.x), self.tets.astype(np.int64)
+        pairs = (t[:, :, None] * nV + t[:, None, :]).reshape(-1)
+        keys = np.unique(np.concatenate([pairs, np.arange(nV, dtype=np.int64) * (nV + 1)]))
+        self.bsr_keys = keys
+        self.bsr_rp = np.ascontiguousarray(np.searchsorted(keys, np.arange(nV + 1, dtype=np.int64) * nV).astype(np.int64))
+        self.bsr_ci = np.ascontiguousarray((keys % nV).astype(np.int32))
+        self.bsr_pos16 = np.ascontiguousarray(np.searchsorted(keys, pairs).astype(np.int64))
+        self.bsr_diag = np.ascontiguousarray(np.searchsorted(keys, np.arange(nV, dtype=np.int64) * (nV + 1)).astype(np.int64))
+
+    def _assemble_bsr(self):
+        nV = len(self.x)
+        n = 3 * nV
+        rhs = -(np.repeat(self.m, 3) * (self.x - self.xTilde).ravel())
+        _, g, H = elasticity(self.tets, self.x, self.Dm, self.la, self.mu, self.dt)
+        dof = (3 * self.tets[:, :, None] + np.arange(3)).reshape(-1, 12)
+        np.add.at(rhs, dof, -g)
+        val = np.zeros((len(self.bsr_keys), 9))
+        lib().oracle_bsr_accumulate(len(self.tets), _p(self.bsr_pos16, np.int64), _p(_f64(H)), _p(val))
+        val[self.bsr_diag, 0] += self.m
+        val[self.bsr_diag, 4] += self.m
+        val[self.bsr_diag, 8] += self.m
+        ck, cv = [], []
+        for k in range(7):
+            r = self.rows[k]
+            if len(r) == 0:
+                continue
+            _, gb, Hb = barrier_rows(k, r, self.x, self.x0, self.dhat2, self.kappa)
+            nv = r.shape[1]
+            dof = (3 * r[:, :, None] + np.arange(3)).reshape(-1, 3 * nv)
+            np.add.at(rhs, dof, -gb)
+            ck.append((r[:, :, None].astype(np.int64) * nV + r[:, None, :]).reshape(-1))
+            cv.append(Hb.reshape(-1, nv, 3, nv, 3).transpose(0, 1, 3, 2, 4).reshape(-1, 9))
+        if ck:
+            ck, cv = np.concatenate(ck), np.concatenate(cv)
+            uk, inv = np.unique(ck, return_inverse=True)
+            cva = np.zeros((len(uk), 9))
+            np.add.at(cva, inv.ravel(), cv)
+        else:
+            uk, cva = np.zeros(0, np.int64), np.zeros((0, 9))
+        self.c_rp = np.ascontiguousarray(np.searchsorted(uk, np.arange(nV + 1, dtype=np.int64) * nV).astype(np.int64))
+        self.c_ci = np.ascontiguousarray((uk % nV).astype(np.int32))
+        self.c_va = np.ascontiguousarray(cva)
+        self.bsr_val = val
+        self.rhs = rhs
+
     # NEWTON_IPC.py:558-747: inertia, elasticity, barriers -> (CSR matrix, rhs)
     def compute_hessian_and_gradient(self):
+        if self.solver == 'bsr':
+            self._tic('Build System')
+            self._assemble_bsr()
+            self._toc('Build System')
+            return None, self.rhs
         import scipy.sparse as sp
         self._tic('Build System')
         n = 3 * len(self.x)
@@ -315,7 +369,16 @@ class OracleSim:
         n = 3 * len(self.x)
         Dm = np.repeat(mask, 3)
         rhs = self.rhs.copy()
-        if self.solver == 'direct':
+        if self.solver == 'bsr':
+            fixed = np.ascontiguousarray(mask.astype(np.uint8))
+            sol = np.zeros(n)
+            it = lib().oracle_bsr_pcg(len(self.x), _p(self.bsr_rp, np.int64), _p(self.bsr_ci, np.int32), _p(self.bsr_val),
+                                      _p(self.c_rp, np.int64), _p(self.c_ci, np.int32), _p(self.c_va),
+                                      _p(self.bsr_diag, np.int64), _p(_f64(rhs)), _p(fixed, np.uint8), D(self.pcg_rtol),
+                                      self.pcg_maxit, _p(sol))
+            self.pcg_iters.append(it)
+            self.sol = sol
+        elif self.solver == 'direct':
             A = self.A.tocoo()
             keep = ~(Dm[A.row] | Dm[A.col])
             A = sp.csr_matrix((A.data * keep, (A.row, A.col)), shape=(n, n))

@@ -65,7 +65,7 @@ def test_barrier_rows_vs_oracle_random(hc, t):
     if t >= 4:
         d = rng.normal(size=(N, 3)) * 3e-3
         X[:, 1] = X[:, 0] + d
-        X[:, 3] = X[:, 2] + d * 1.05 + rng.normal(size=(N, 3)) * 1e-6
+        X[:, 3] = X[:, 2] + d * 1.05 + rng.normal(size=(N, 3)) * 3e-5   # ~1e-2 rad: inside the mollifier band
     X0 = X.copy()
     X0[:, 1] = X0[:, 0] + (X[:, 1] - X[:, 0]) * 4
     X0[:, 3] = X0[:, 2] + (X[:, 3] - X[:, 2]) * 4
