@@ -20,6 +20,7 @@ int check_collision(fipc_ctx* c, const double* x, int* hit_h, cudaStream_t s);
 int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t s);
 int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* diag_pos, double rtol, int maxit, double* sol, int* iters,
               cudaStream_t s);
+int sell_to_bsr(fipc_ctx* c, double* out, cudaStream_t s);
 int launch_energy(const fipc_ctx* c, const double* x, const double* xt, const int* const* rows, const int* counts, double* part,
                   double* out, cudaStream_t s);
 int launch_absmax(int n, const double* p, double* part, double* out, cudaStream_t s);
@@ -45,7 +46,8 @@ double det3h(const double* A) {
 void free_ctx(fipc_ctx* c) {
     void* ptrs[] = {c->tets, c->bp, c->be, c->bt, c->dminv, c->vol, c->lam, c->mu, c->mass, c->x0, c->row_ptr, c->col_idx,
                     c->up_pos, c->up_tpos, c->up_row, c->up_cptr, c->up_contrib, c->vt_ptr, c->vt_list, c->elem_g, c->elem_H,
-                    c->bsr_val, c->rhs, c->d_counts, c->diag_pos};
+                    c->bsr_val, c->rhs, c->d_counts, c->diag_pos, c->sell_off, c->sell_col, c->row_len, c->bsr2sell,
+                    c->up_spos, c->up_tspos, c->diag_spos, c->sell_val};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int t = 0; t < N_TYPES; ++t) c->rows[t].release();
@@ -199,6 +201,36 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
     }
     std::vector<int> diag_pos(n_verts);
     for (int i = 0; i < n_verts; ++i) diag_pos[i] = pos_of(i, i);
+    // sliced-ELL layout of the same pattern
+    const int n_slices = (n_verts + 31) / 32;
+    std::vector<int> sell_off(n_slices + 1, 0), row_len(32ull * n_slices, 0);
+    for (int i = 0; i < n_verts; ++i) row_len[i] = row_ptr[i + 1] - row_ptr[i];
+    for (int sl = 0; sl < n_slices; ++sl) {
+        int mx = 0;
+        for (int l = 0; l < 32; ++l) mx = std::max(mx, row_len[32 * sl + l]);
+        sell_off[sl + 1] = sell_off[sl] + mx;
+    }
+    const long long n_slots = sell_off[n_slices];
+    std::vector<int> sell_col(32ull * n_slots, 0), bsr2sell(nnzb);
+    for (int i = 0; i < n_verts; ++i) {
+        const int sl = i >> 5, lane = i & 31;
+        for (int k = 0; k < row_len[i]; ++k) {
+            const long long slot = sell_off[sl] + k;
+            sell_col[slot * 32 + lane] = col_idx[row_ptr[i] + k];
+            bsr2sell[row_ptr[i] + k] = (int)(slot * 32 + lane);
+        }
+        for (int k = row_len[i]; k < sell_off[sl + 1] - sell_off[sl]; ++k) sell_col[(sell_off[sl] + k) * 32 + lane] = i;
+    }
+    if (32ll * n_slots >= (1ll << 31)) {
+        free_ctx(c);
+        return FIPC_ERR_CAPACITY;
+    }
+    std::vector<int> up_spos(n_upper), up_tspos(n_upper), diag_spos(n_verts);
+    for (int u = 0; u < n_upper; ++u) {
+        up_spos[u] = bsr2sell[up_pos[u]];
+        up_tspos[u] = bsr2sell[up_tpos[u]];
+    }
+    for (int i = 0; i < n_verts; ++i) diag_spos[i] = bsr2sell[diag_pos[i]];
 
     int st = FIPC_OK;
     st |= upload(&c->tets, tets, 4ull * n_tets);
@@ -221,12 +253,23 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
     st |= upload(&c->vt_ptr, vt_ptr.data(), vt_ptr.size());
     st |= upload(&c->vt_list, vt_list.data(), vt_list.size());
     st |= upload(&c->diag_pos, diag_pos.data(), diag_pos.size());
+    st |= upload(&c->sell_off, sell_off.data(), sell_off.size());
+    st |= upload(&c->sell_col, sell_col.data(), sell_col.size());
+    st |= upload(&c->row_len, row_len.data(), row_len.size());
+    st |= upload(&c->bsr2sell, bsr2sell.data(), bsr2sell.size());
+    st |= upload(&c->up_spos, up_spos.data(), up_spos.size());
+    st |= upload(&c->up_tspos, up_tspos.data(), up_tspos.size());
+    st |= upload(&c->diag_spos, diag_spos.data(), diag_spos.size());
+    c->n_slices = n_slices;
+    c->n_slots = n_slots;
     c->nnzb = (int)nnzb;
     c->n_upper = n_upper;
     if (st == FIPC_OK) {
         if (cudaMalloc((void**)&c->elem_g, sizeof(double) * 12ull * (n_tets > 0 ? n_tets : 1)) != cudaSuccess ||
             cudaMalloc((void**)&c->elem_H, sizeof(double) * 90ull * (n_tets > 0 ? n_tets : 1)) != cudaSuccess ||
             cudaMalloc((void**)&c->bsr_val, sizeof(double) * 9ull * nnzb) != cudaSuccess ||
+            cudaMalloc((void**)&c->sell_val, sizeof(double) * 288ull * (n_slots > 0 ? n_slots : 1)) != cudaSuccess ||
+            cudaMemset(c->sell_val, 0, sizeof(double) * 288ull * (n_slots > 0 ? n_slots : 1)) != cudaSuccess ||
             cudaMalloc((void**)&c->rhs, sizeof(double) * 3ull * n_verts) != cudaSuccess ||
             cudaMalloc((void**)&c->d_counts, sizeof(int) * (N_TYPES + 1)) != cudaSuccess)
             st = FIPC_ERR_CUDA;
@@ -308,7 +351,10 @@ int fipc_export_system(fipc_ctx* c, int* row_ptr, int* col_idx, double* val, int
     cudaStream_t s = (cudaStream_t)stream;
     if (row_ptr) FIPC_CUDA(cudaMemcpyAsync(row_ptr, c->row_ptr, 4ll * (c->nV + 1), cudaMemcpyDeviceToDevice, s));
     if (col_idx) FIPC_CUDA(cudaMemcpyAsync(col_idx, c->col_idx, 4ll * c->nnzb, cudaMemcpyDeviceToDevice, s));
-    if (val) FIPC_CUDA(cudaMemcpyAsync(val, c->bsr_val, 72ll * c->nnzb, cudaMemcpyDeviceToDevice, s));
+    if (val) {
+        const int st = sell_to_bsr(c, val, s);
+        if (st) return st;
+    }
     if (c_row_ptr) {
         if (c->c_nnzb) FIPC_CUDA(cudaMemcpyAsync(c_row_ptr, c->c_rowptr.p, 4ll * (c->nV + 1), cudaMemcpyDeviceToDevice, s));
         else FIPC_CUDA(cudaMemsetAsync(c_row_ptr, 0, 4ll * (c->nV + 1), s));
@@ -319,8 +365,10 @@ int fipc_export_system(fipc_ctx* c, int* row_ptr, int* col_idx, double* val, int
     return FIPC_OK;
 }
 
-int fipc_solve_system(fipc_ctx* c, const unsigned char* fixed, double rtol, int maxit, double* sol, int* iters_h, void* stream) {
+int fipc_solve_system(fipc_ctx* c, const unsigned char* fixed, double rtol, int maxit, int use_guess, double* sol, int* iters_h,
+                      void* stream) {
     if (!c || !fixed || !sol || maxit <= 0 || !(rtol >= 0)) return FIPC_ERR_ARGUMENT;
+    if (!use_guess) FIPC_CUDA(cudaMemsetAsync(sol, 0, sizeof(double) * 3ull * c->nV, (cudaStream_t)stream));
     return pcg_solve(c, fixed, c->diag_pos, rtol, maxit, sol, iters_h, (cudaStream_t)stream);
 }
 

@@ -68,6 +68,15 @@ struct fipc_ctx_impl {
     int *up_pos = nullptr, *up_tpos = nullptr, *up_row = nullptr, *up_cptr = nullptr, *up_contrib = nullptr;
     int *vt_ptr = nullptr, *vt_list = nullptr;   // vertex -> (tet*4 + local) for the gradient gather
     int* diag_pos = nullptr;                     // BSR position of each vertex's diagonal block
+    // the same matrix in sliced-ELL form (32 rows per slice, blocks of a slice stored
+    // column-major so that each of the 9 block entries loads as one coalesced 256-byte row):
+    // slot (slice s, k) = sell_off[s] + k; its column ids at sell_col[slot*32 + lane] and its
+    // values at sell_val[slot*288 + entry*32 + lane]; padding slots have row_len <= k
+    int n_slices = 0;
+    long long n_slots = 0;
+    int *sell_off = nullptr, *sell_col = nullptr, *row_len = nullptr, *bsr2sell = nullptr;
+    int *up_spos = nullptr, *up_tspos = nullptr, *diag_spos = nullptr;
+    double* sell_val = nullptr;
     // per-iteration element data and the system
     double *elem_g = nullptr, *elem_H = nullptr, *bsr_val = nullptr, *rhs = nullptr;
     // constraint lists (capacity rows of 4 ints each) and counts

@@ -23,8 +23,14 @@
 namespace fipc {
 
 // ---------------------------------------------------------------- elastic + inertia
+__device__ __forceinline__ double* sell_block(double* val, int enc) {
+    return val + (size_t)(enc >> 5) * 288 + (enc & 31);
+}
+
+// one thread per upper block: fixed-order sum of its contributions, written to (i,j) and
+// transposed to (j,i) in the sliced-ELL value array (entry stride 32)
 __global__ void k_assemble_elastic(int n_upper, const int* __restrict__ cptr, const int* __restrict__ contrib,
-                                   const int* __restrict__ pos, const int* __restrict__ tpos, const int* __restrict__ urow,
+                                   const int* __restrict__ spos, const int* __restrict__ tspos, const int* __restrict__ urow,
                                    const double* __restrict__ elem_H, const double* __restrict__ mass, double* __restrict__ val) {
     const int u = blockIdx.x * blockDim.x + threadIdx.x;
     if (u >= n_upper) return;
@@ -42,21 +48,32 @@ __global__ void k_assemble_elastic(int n_upper, const int* __restrict__ cptr, co
             for (int i = 0; i < 9; ++i) s[i] += H[i];
         }
     }
-    const int p = pos[u], q = tpos[u];
+    const int p = spos[u], q = tspos[u];
     if (p == q) {
         const double m = mass[urow[u]];
         s[0] += m;
         s[4] += m;
         s[8] += m;
     }
+    double* dp = sell_block(val, p);
 #pragma unroll
-    for (int i = 0; i < 9; ++i) val[9 * (size_t)p + i] = s[i];
+    for (int i = 0; i < 9; ++i) dp[32 * i] = s[i];
     if (p != q) {
+        double* dq = sell_block(val, q);
 #pragma unroll
         for (int i = 0; i < 3; ++i)
 #pragma unroll
-            for (int j = 0; j < 3; ++j) val[9 * (size_t)q + i * 3 + j] = s[j * 3 + i];
+            for (int j = 0; j < 3; ++j) dq[32 * (i * 3 + j)] = s[j * 3 + i];
     }
+}
+
+// sliced-ELL -> block-CSR order (export for tests)
+__global__ void k_sell_to_bsr(int nnzb, const int* __restrict__ bsr2sell, const double* __restrict__ sval, double* __restrict__ bval) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nnzb) return;
+    const double* src = sval + (size_t)(bsr2sell[k] >> 5) * 288 + (bsr2sell[k] & 31);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) bval[9 * (size_t)k + i] = src[32 * i];
 }
 
 // rhs = -(m (x - xt) + sum of element gradients)   (NEWTON_IPC.py:558-567, 679-690)
@@ -153,211 +170,223 @@ __global__ void k_contact_rowptr(int nV, int nu, const unsigned long long* __res
 }
 
 // ---------------------------------------------------------------- PCG
+// Chronopoulos-Gear form of preconditioned CG: per iteration one SpMV w = A u (u = M^-1 r,
+// already formed) fused with the three dot products (r,u), (w,u), (r,r), and one vector update
+//   p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s, u = M^-1 r.
+// Dot products: per-block partials; the last block to finish (atomic ticket) sums them in block
+// order and derives alpha/beta, so the scalars are bitwise reproducible and need no launch.
 struct PCGArgs {
     int nV;
-    const int *rp, *ci;          // elastic BSR
-    const double* va;
-    const int *crp, *cci;        // contact BSR
+    const int *soff, *scol, *rlen;   // elastic matrix, sliced-ELL
+    const double* sval;
+    const int *crp, *cci;            // contact matrix, block-CSR
     const double* cva;
     const unsigned char* fixed;
-    double *x, *r, *z, *p0, *p1, *ap, *minv;
-    double *part;                // [5][RED_BLOCKS]: rz(2), rr(2), pAp
-    double* sc;                  // [0] rz_prev, [1] rr0, [2] rtol^2
-    int* flag;                   // [0] done, [1] iterations
+    const int* diag_spos;
+    double *x, *r, *u, *w, *p, *s, *minv;
+    double* part;                    // [3][nblk]
+    double* sc;                      // scalars, see SC_*
+    int* flag;                       // [0] done, [1] iterations, [2] ticket
 };
+enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
+constexpr int PCG_THREADS = 128;
 
-__device__ __forceinline__ double sum_parts(const double* __restrict__ p, double* sh) {
-    double a = 0.0;
-    for (int i = threadIdx.x; i < RED_BLOCKS; i += blockDim.x) a += p[i];
-    sh[threadIdx.x] = a;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
+// w_i = sum_j A_ij v_j over the elastic (sliced-ELL) and contact (block-CSR) rows of vertex i
+__device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double* __restrict__ v, double& y0, double& y1, double& y2) {
+    y0 = y1 = y2 = 0.0;
+    const int sl = i >> 5, lane = i & 31;
+    const int base = a.soff[sl], len = a.rlen[i];
+    for (int k = 0; k < len; ++k) {
+        const size_t slot = (size_t)(base + k);
+        const int j = __ldg(a.scol + slot * 32 + lane);
+        const double* B = a.sval + slot * 288 + lane;
+        const double v0 = __ldg(v + 3 * j), v1 = __ldg(v + 3 * j + 1), v2 = __ldg(v + 3 * j + 2);
+        y0 += __ldg(B + 0) * v0 + __ldg(B + 32) * v1 + __ldg(B + 64) * v2;
+        y1 += __ldg(B + 96) * v0 + __ldg(B + 128) * v1 + __ldg(B + 160) * v2;
+        y2 += __ldg(B + 192) * v0 + __ldg(B + 224) * v1 + __ldg(B + 256) * v2;
     }
-    const double r = sh[0];
+    for (int e = a.crp[i]; e < a.crp[i + 1]; ++e) {
+        const int j = a.cci[e];
+        const double* B = a.cva + 9 * (size_t)e;
+        const double v0 = v[3 * j], v1 = v[3 * j + 1], v2 = v[3 * j + 2];
+        y0 += B[0] * v0 + B[1] * v1 + B[2] * v2;
+        y1 += B[3] * v0 + B[4] * v1 + B[5] * v2;
+        y2 += B[6] * v0 + B[7] * v1 + B[8] * v2;
+    }
+}
+
+// block sums of up to 3 values into part[c * nblk + block]; returns true in every thread of
+// the last block to finish, which then reduces the partials with final_sums
+template <int NV>
+__device__ __forceinline__ bool block_partials(const PCGArgs& a, const double (&v)[NV]) {
+    __shared__ double sh[NV][PCG_THREADS / 32];
+    __shared__ bool last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        double x = v[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[c][wid] = x;
+    }
     __syncthreads();
-    return r;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+            double t = 0.0;
+            for (int k = 0; k < PCG_THREADS / 32; ++k) t += sh[c][k];
+            a.part[c * gridDim.x + blockIdx.x] = t;
+        }
+        __threadfence();
+        const int ticket = atomicAdd(&a.flag[2], 1);
+        last = ticket == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    return last;
 }
 
-__device__ __forceinline__ void inv3x3(const double* A, double* R) {
-    const double c00 = A[4] * A[8] - A[5] * A[7], c01 = A[5] * A[6] - A[3] * A[8], c02 = A[3] * A[7] - A[4] * A[6];
-    const double det = A[0] * c00 + A[1] * c01 + A[2] * c02, id = 1.0 / det;
-    R[0] = c00 * id;
-    R[1] = (A[2] * A[7] - A[1] * A[8]) * id;
-    R[2] = (A[1] * A[5] - A[2] * A[4]) * id;
-    R[3] = c01 * id;
-    R[4] = (A[0] * A[8] - A[2] * A[6]) * id;
-    R[5] = (A[2] * A[3] - A[0] * A[5]) * id;
-    R[6] = c02 * id;
-    R[7] = (A[1] * A[6] - A[0] * A[7]) * id;
-    R[8] = (A[0] * A[4] - A[1] * A[3]) * id;
+// in the last block: out[c] = sum over blocks of part[c * nblk + b], every thread striding the
+// blocks in a fixed order and a fixed shuffle/shared tree (bitwise reproducible)
+template <int NV>
+__device__ __forceinline__ void final_sums(const PCGArgs& a, double (&out)[NV]) {
+    __shared__ double sh[NV][PCG_THREADS / 32];
+    __threadfence();
+    const int nb = gridDim.x, lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        double t = 0.0;
+        for (int b = threadIdx.x; b < nb; b += PCG_THREADS) t += *(volatile double*)&a.part[c * nb + b];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) sh[c][wid] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int c = 0; c < NV; ++c) {
+        double t = 0.0;
+        for (int k = 0; k < PCG_THREADS / 32; ++k) t += sh[c][k];
+        out[c] = t;
+    }
 }
 
-// setup: M^-1 from diagonal blocks, x = 0, r = masked rhs, z = M^-1 r, partials of r.z, r.r
-__global__ void __launch_bounds__(RED_THREADS) k_pcg_init(PCGArgs a, const double* __restrict__ rhs, const int* __restrict__ diag_pos) {
-    __shared__ double sh[RED_THREADS];
-    double rz = 0.0, rr = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nV; i += gridDim.x * blockDim.x) {
-        double D[9], Mi[9];
+// residual of the initial guess, block-Jacobi inverse, u = M^-1 r; partials of (r,r)
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const double* __restrict__ rhs, double rtol) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0;
+    if (i < a.nV) {
+        double Mi[9];
         const bool fx = a.fixed[i] != 0;
         if (fx) {
             for (int k = 0; k < 9; ++k) Mi[k] = (k % 4 == 0) ? 1.0 : 0.0;
         } else {
-            const double* E = a.va + 9 * (size_t)diag_pos[i];
-            for (int k = 0; k < 9; ++k) D[k] = E[k];
+            double D[9];
+            const double* E = a.sval + (size_t)(a.diag_spos[i] >> 5) * 288 + (a.diag_spos[i] & 31);
+            for (int k = 0; k < 9; ++k) D[k] = E[32 * k];
             for (int k = a.crp[i]; k < a.crp[i + 1]; ++k)
                 if (a.cci[k] == i)
                     for (int q = 0; q < 9; ++q) D[q] += a.cva[9 * (size_t)k + q];
-            inv3x3(D, Mi);
+            const double c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8], c02 = D[3] * D[7] - D[4] * D[6];
+            const double id = 1.0 / (D[0] * c00 + D[1] * c01 + D[2] * c02);
+            Mi[0] = c00 * id;
+            Mi[1] = (D[2] * D[7] - D[1] * D[8]) * id;
+            Mi[2] = (D[1] * D[5] - D[2] * D[4]) * id;
+            Mi[3] = c01 * id;
+            Mi[4] = (D[0] * D[8] - D[2] * D[6]) * id;
+            Mi[5] = (D[2] * D[3] - D[0] * D[5]) * id;
+            Mi[6] = c02 * id;
+            Mi[7] = (D[1] * D[6] - D[0] * D[7]) * id;
+            Mi[8] = (D[0] * D[4] - D[1] * D[3]) * id;
         }
         for (int k = 0; k < 9; ++k) a.minv[9 * (size_t)i + k] = Mi[k];
-        double r3[3];
+        double y0, y1, y2;
+        row_apply(a, i, a.x, y0, y1, y2);
+        const double r0 = fx ? 0.0 : rhs[3 * i] - y0, r1 = fx ? 0.0 : rhs[3 * i + 1] - y1, r2 = fx ? 0.0 : rhs[3 * i + 2] - y2;
+        a.r[3 * i] = r0;
+        a.r[3 * i + 1] = r1;
+        a.r[3 * i + 2] = r2;
         for (int d = 0; d < 3; ++d) {
-            r3[d] = fx ? 0.0 : rhs[3 * i + d];
-            a.r[3 * i + d] = r3[d];
-            a.x[3 * i + d] = 0.0;
-            a.p1[3 * i + d] = 0.0;
+            a.u[3 * i + d] = Mi[3 * d] * r0 + Mi[3 * d + 1] * r1 + Mi[3 * d + 2] * r2;
+            a.p[3 * i + d] = 0.0;
+            a.s[3 * i + d] = 0.0;
         }
-        for (int d = 0; d < 3; ++d) {
-            const double zd = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
-            a.z[3 * i + d] = zd;
-            rz += r3[d] * zd;
-            rr += r3[d] * r3[d];
-        }
+        rr = r0 * r0 + r1 * r1 + r2 * r2;
     }
-    sh[threadIdx.x] = rz;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) a.part[0 * RED_BLOCKS + blockIdx.x] = sh[0];
-    __syncthreads();
-    sh[threadIdx.x] = rr;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) a.part[2 * RED_BLOCKS + blockIdx.x] = sh[0];
-}
-
-__global__ void k_pcg_init_scalars(PCGArgs a, double rtol) {
-    __shared__ double sh[RED_THREADS];
-    const double rr0 = sum_parts(a.part + 2 * RED_BLOCKS, sh);
-    if (threadIdx.x == 0) {
-        a.sc[0] = 1.0;
-        a.sc[1] = rr0;
-        a.sc[2] = rtol * rtol * rr0;
-        a.flag[0] = rr0 == 0.0 ? 1 : 0;
+    const double v[1] = {rr};
+    if (block_partials<1>(a, v)) {
+        double tt[1];
+        final_sums<1>(a, tt);
+        if (threadIdx.x != 0) return;
+        const double t = tt[0];
+        a.sc[SC_RR0] = t;
+        a.sc[SC_TOL2] = rtol * rtol * t;
+        a.sc[SC_GAMMA] = 1.0;
+        a.sc[SC_ALPHA] = 1.0;
+        a.flag[0] = t == 0.0 ? 1 : 0;
         a.flag[1] = 0;
+        a.flag[2] = 0;
     }
 }
 
-// K1 of iteration k: beta, p_k = z + beta p_{k-1}, Ap = A p_k (masked), partials of p.Ap
-__global__ void __launch_bounds__(RED_THREADS) k_pcg_spmv(PCGArgs a, int k) {
-    __shared__ double sh[RED_THREADS];
+// iteration k, part 1: w = A u and the dot products; the last block derives alpha, beta
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_spmv(PCGArgs a, int k) {
     if (*(volatile int*)&a.flag[0]) return;
-    const int par = k & 1;
-    const double rz = sum_parts(a.part + par * RED_BLOCKS, sh);
-    const double rr = sum_parts(a.part + (2 + par) * RED_BLOCKS, sh);
-    if (rr <= a.sc[2]) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double g = 0.0, dl = 0.0, rr = 0.0;
+    if (i < a.nV) {
+        double y0 = 0.0, y1 = 0.0, y2 = 0.0;
+        if (!a.fixed[i]) row_apply(a, i, a.u, y0, y1, y2);
+        a.w[3 * i] = y0;
+        a.w[3 * i + 1] = y1;
+        a.w[3 * i + 2] = y2;
+        const double u0 = a.u[3 * i], u1 = a.u[3 * i + 1], u2 = a.u[3 * i + 2];
+        const double r0 = a.r[3 * i], r1 = a.r[3 * i + 1], r2 = a.r[3 * i + 2];
+        g = r0 * u0 + r1 * u1 + r2 * u2;
+        dl = y0 * u0 + y1 * u1 + y2 * u2;
+        rr = r0 * r0 + r1 * r1 + r2 * r2;
+    }
+    const double v[3] = {g, dl, rr};
+    if (block_partials<3>(a, v)) {
+        double tt[3];
+        final_sums<3>(a, tt);
+        if (threadIdx.x != 0) return;
+        const double G = tt[0], Dl = tt[1], R = tt[2];
+        a.flag[2] = 0;
+        if (R <= a.sc[SC_TOL2]) {
             a.flag[0] = 1;
             a.flag[1] = k;
+            return;
         }
-        return;
+        const double beta = k == 0 ? 0.0 : G / a.sc[SC_GAMMA];
+        const double alpha = k == 0 ? G / Dl : G / (Dl - beta * G / a.sc[SC_ALPHA]);
+        a.sc[SC_GAMMA] = G;
+        a.sc[SC_DELTA] = Dl;
+        a.sc[SC_RR] = R;
+        a.sc[SC_BETA] = beta;
+        a.sc[SC_ALPHA] = alpha;
     }
-    const double beta = k == 0 ? 0.0 : rz / a.sc[0];
-    const double* pp = (k & 1) ? a.p0 : a.p1;   // p_{k-1}
-    double* pn = (k & 1) ? a.p1 : a.p0;         // p_k
-    double acc = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nV; i += gridDim.x * blockDim.x) {
-        double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-        const double q0 = a.z[3 * i] + beta * pp[3 * i], q1 = a.z[3 * i + 1] + beta * pp[3 * i + 1],
-                     q2 = a.z[3 * i + 2] + beta * pp[3 * i + 2];
-        pn[3 * i] = q0;
-        pn[3 * i + 1] = q1;
-        pn[3 * i + 2] = q2;
-        if (!a.fixed[i]) {
-            for (int e = a.rp[i]; e < a.rp[i + 1]; ++e) {
-                const int j = a.ci[e];
-                const double* B = a.va + 9 * (size_t)e;
-                const double p0 = a.z[3 * j] + beta * pp[3 * j], p1 = a.z[3 * j + 1] + beta * pp[3 * j + 1],
-                             p2 = a.z[3 * j + 2] + beta * pp[3 * j + 2];
-                y0 += B[0] * p0 + B[1] * p1 + B[2] * p2;
-                y1 += B[3] * p0 + B[4] * p1 + B[5] * p2;
-                y2 += B[6] * p0 + B[7] * p1 + B[8] * p2;
-            }
-            for (int e = a.crp[i]; e < a.crp[i + 1]; ++e) {
-                const int j = a.cci[e];
-                const double* B = a.cva + 9 * (size_t)e;
-                const double p0 = a.z[3 * j] + beta * pp[3 * j], p1 = a.z[3 * j + 1] + beta * pp[3 * j + 1],
-                             p2 = a.z[3 * j + 2] + beta * pp[3 * j + 2];
-                y0 += B[0] * p0 + B[1] * p1 + B[2] * p2;
-                y1 += B[3] * p0 + B[4] * p1 + B[5] * p2;
-                y2 += B[6] * p0 + B[7] * p1 + B[8] * p2;
-            }
-        }
-        a.ap[3 * i] = y0;
-        a.ap[3 * i + 1] = y1;
-        a.ap[3 * i + 2] = y2;
-        acc += q0 * y0 + q1 * y1 + q2 * y2;
-    }
-    sh[threadIdx.x] = acc;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) a.part[4 * RED_BLOCKS + blockIdx.x] = sh[0];
 }
 
-// K2 of iteration k: alpha, x += alpha p, r -= alpha Ap, z = M^-1 r, partials of r.z, r.r
-__global__ void __launch_bounds__(RED_THREADS) k_pcg_update(PCGArgs a, int k) {
-    __shared__ double sh[RED_THREADS];
+// iteration k, part 2: recurrences and the preconditioner
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_update(PCGArgs a) {
     if (*(volatile int*)&a.flag[0]) return;
-    const int par = k & 1;
-    const double rz = sum_parts(a.part + par * RED_BLOCKS, sh);
-    const double pAp = sum_parts(a.part + 4 * RED_BLOCKS, sh);
-    const double alpha = rz / pAp;
-    const double* pk = (k & 1) ? a.p1 : a.p0;
-    double rzn = 0.0, rrn = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nV; i += gridDim.x * blockDim.x) {
-        double r3[3];
-        for (int d = 0; d < 3; ++d) {
-            a.x[3 * i + d] += alpha * pk[3 * i + d];
-            r3[d] = a.r[3 * i + d] - alpha * a.ap[3 * i + d];
-            a.r[3 * i + d] = r3[d];
-        }
-        const double* Mi = a.minv + 9 * (size_t)i;
-        for (int d = 0; d < 3; ++d) {
-            const double zd = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
-            a.z[3 * i + d] = zd;
-            rzn += r3[d] * zd;
-            rrn += r3[d] * r3[d];
-        }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nV) return;
+    const double alpha = a.sc[SC_ALPHA], beta = a.sc[SC_BETA];
+    double r3[3];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        const int q = 3 * i + d;
+        const double p = a.u[q] + beta * a.p[q];
+        const double s = a.w[q] + beta * a.s[q];
+        a.p[q] = p;
+        a.s[q] = s;
+        a.x[q] += alpha * p;
+        r3[d] = a.r[q] - alpha * s;
+        a.r[q] = r3[d];
     }
-    const int npar = (k + 1) & 1;
-    sh[threadIdx.x] = rzn;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) a.part[npar * RED_BLOCKS + blockIdx.x] = sh[0];
-    __syncthreads();
-    sh[threadIdx.x] = rrn;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        a.part[(2 + npar) * RED_BLOCKS + blockIdx.x] = sh[0];
-        if (blockIdx.x == 0) a.sc[0] = rz;
-    }
+    const double* Mi = a.minv + 9 * (size_t)i;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) a.u[3 * i + d] = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
 }
 
 // ---------------------------------------------------------------- host side
@@ -382,8 +411,8 @@ int launch_barrier_rows(int type, int n, const int* rows, const double* x, const
 int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t s) {
     int st = launch_elasticity(c->nT, c->tets, x, c->dminv, c->vol, c->lam, c->mu, c->dt, nullptr, c->elem_g, c->elem_H, s);
     if (st) return st;
-    k_assemble_elastic<<<nblk(c->n_upper, 128), 128, 0, s>>>(c->n_upper, c->up_cptr, c->up_contrib, c->up_pos, c->up_tpos, c->up_row,
-                                                             c->elem_H, c->mass, c->bsr_val);
+    k_assemble_elastic<<<nblk(c->n_upper, 128), 128, 0, s>>>(c->n_upper, c->up_cptr, c->up_contrib, c->up_spos, c->up_tspos,
+                                                             c->up_row, c->elem_H, c->mass, c->sell_val);
     FIPC_LAUNCHED();
     k_assemble_rhs<<<nblk(c->nV, 128), 128, 0, s>>>(c->nV, c->vt_ptr, c->vt_list, c->elem_g, c->mass, x, xt, c->rhs);
     FIPC_LAUNCHED();
@@ -457,58 +486,68 @@ int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t
     return FIPC_OK;
 }
 
-// solve_system (NEWTON_IPC.py:750-777) by block-Jacobi PCG; sol: device [3 nV]
-int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* diag_pos, double rtol, int maxit, double* sol, int* iters,
+int sell_to_bsr(fipc_ctx* c, double* out, cudaStream_t s) {
+    k_sell_to_bsr<<<nblk(c->nnzb, 256), 256, 0, s>>>(c->nnzb, c->bsr2sell, c->sell_val, out);
+    FIPC_LAUNCHED();
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+
+// solve_system (NEWTON_IPC.py:750-777) by block-Jacobi PCG; sol: device [3 nV] holding the
+// initial guess on entry (zero for the reference's semantics) and the solution on return
+int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, double rtol, int maxit, double* sol, int* iters,
               cudaStream_t s) {
     const long long n3 = 3ll * c->nV;
-    if (c->pcg_vec.ensure(8 * (n3 * 6 + 9ll * c->nV)) || c->pcg_part.ensure(8ll * 5 * RED_BLOCKS + 64) || c->scal.ensure(64))
+    const int nb = nblk(c->nV, PCG_THREADS);
+    if (c->pcg_vec.ensure(8 * (n3 * 6 + 9ll * c->nV)) || c->pcg_part.ensure(8ll * (3 * nb + SC_COUNT) + 64) || c->scal.ensure(64))
         return FIPC_ERR_CUDA;
     if (c->c_nnzb == 0 && (c->c_rowptr.ensure(4ll * (c->nV + 1)) || cudaMemsetAsync(c->c_rowptr.p, 0, 4ll * (c->nV + 1), s)))
         return FIPC_ERR_CUDA;
     if (c->c_val.ensure(72) || c->c_col.ensure(4)) return FIPC_ERR_CUDA;
     PCGArgs a;
     a.nV = c->nV;
-    a.rp = c->row_ptr;
-    a.ci = c->col_idx;
-    a.va = c->bsr_val;
+    a.soff = c->sell_off;
+    a.scol = c->sell_col;
+    a.rlen = c->row_len;
+    a.sval = c->sell_val;
     a.crp = c->c_rowptr.as<int>();
     a.cci = c->c_col.as<int>();
     a.cva = c->c_val.as<double>();
     a.fixed = fixed;
+    a.diag_spos = c->diag_spos;
     double* v = c->pcg_vec.as<double>();
     a.x = sol;
     a.r = v;
-    a.z = v + n3;
-    a.p0 = v + 2 * n3;
-    a.p1 = v + 3 * n3;
-    a.ap = v + 4 * n3;
+    a.u = v + n3;
+    a.w = v + 2 * n3;
+    a.p = v + 3 * n3;
+    a.s = v + 4 * n3;
     a.minv = v + 5 * n3;
     a.part = c->pcg_part.as<double>();
-    a.sc = c->pcg_part.as<double>() + 5 * RED_BLOCKS;
+    a.sc = a.part + 3 * nb;
     a.flag = (int*)(c->scal.as<char>() + 48);
-    k_pcg_init<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, c->rhs, diag_pos);
-    FIPC_LAUNCHED();
-    k_pcg_init_scalars<<<1, RED_THREADS, 0, s>>>(a, rtol);
+    FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 3 * sizeof(int), s));
+    // traffic model per launch: matrix blocks and column ids once (padding slots included),
+    // row data, the gathered vector once, w written, r read
+    const double slots = 32.0 * (double)c->n_slots, nv = (double)c->nV, cn = (double)c->c_nnzb;
+    const double spmv_bytes = slots * (72.0 + 4.0) + cn * 76.0 + nv * (4.0 + 4.0 + 1.0 + 24.0 + 24.0 + 24.0);
+    const double spmv_flops = (double)(c->nnzb + c->c_nnzb) * 18.0 + nv * 18.0;
+    const double upd_bytes = nv * (24.0 * 2 + 24.0 * 2 * 4 + 24.0 + 72.0);
+    const double upd_flops = nv * 36.0;
+    k_pcg_start<<<nb, PCG_THREADS, 0, s>>>(a, c->rhs, rtol);
     FIPC_LAUNCHED();
     int h_flag[2] = {0, 0};
-    const int chunk = 32;
-    // algorithmic traffic per launch: every matrix block and column index once, the vertex
-    // vectors once each (z and p_{k-1} read, p_k and Ap written), row pointers and flags
-    const double nnz = (double)c->nnzb + (double)c->c_nnzb, nv = (double)c->nV;
-    const double spmv_bytes = nnz * 76.0 + nv * (4.0 + 4.0 + 1.0 + 4 * 24.0);
-    const double spmv_flops = nnz * 24.0 + nv * 12.0;
-    const double upd_bytes = nv * (2 * 24.0 + 2 * 24.0 + 24.0 + 24.0 + 24.0 + 72.0);
-    const double upd_flops = nv * 42.0;
+    const int chunk = 64;
     for (int k0 = 0; k0 < maxit; k0 += chunk) {
         for (int k = k0; k < k0 + chunk && k < maxit; ++k) {
             {
                 ProfScope ps(PK_PCG_SPMV, s, spmv_bytes, spmv_flops);
-                k_pcg_spmv<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, k);
+                k_pcg_spmv<<<nb, PCG_THREADS, 0, s>>>(a, k);
             }
             FIPC_LAUNCHED();
             {
                 ProfScope ps(PK_PCG_UPDATE, s, upd_bytes, upd_flops);
-                k_pcg_update<<<RED_BLOCKS, RED_THREADS, 0, s>>>(a, k);
+                k_pcg_update<<<nb, PCG_THREADS, 0, s>>>(a);
             }
             FIPC_LAUNCHED();
         }

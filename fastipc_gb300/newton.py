@@ -190,7 +190,7 @@ class NewtonIPC:
         with self.timer('Solve System'):
             self._dirichlet(t)
             it = ctypes.c_int()
-            st = N.lib().fipc_solve_system(self.ctx, dptr(self.fixed, torch.uint8), D(self.pcg_rtol), self.pcg_maxit,
+            st = N.lib().fipc_solve_system(self.ctx, dptr(self.fixed, torch.uint8), D(self.pcg_rtol), self.pcg_maxit, 0,
                                            dptr(self.data_sol, F64), ctypes.byref(it), self._s())
             check(st, 'solve_system')
             self.pcg_iters.append(it.value)

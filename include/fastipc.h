@@ -84,9 +84,11 @@ int fipc_export_system(fipc_ctx* ctx, int* row_ptr, int* col_idx, double* val, i
                        double* c_val, double* rhs, void* stream);
 
 /* solve_system, NEWTON_IPC.py:750-777: Newton direction with Dirichlet vertices (fixed [V])
- * held at zero, by block-Jacobi PCG to relative residual rtol (iters_h: iterations used). */
-int fipc_solve_system(fipc_ctx* ctx, const unsigned char* fixed, double rtol, int maxit, double* sol, int* iters_h,
-                      void* stream);
+ * held at zero, by block-Jacobi PCG to relative residual rtol (iters_h: iterations used).
+ * use_guess = 0 starts from zero (the reference's semantics); otherwise sol holds the
+ * initial guess on entry. */
+int fipc_solve_system(fipc_ctx* ctx, const unsigned char* fixed, double rtol, int maxit, int use_guess, double* sol,
+                      int* iters_h, void* stream);
 
 /* output_residual, NEWTON_IPC.py:805-812: max |sol| */
 int fipc_output_residual(fipc_ctx* ctx, const double* sol, double* res_h, void* stream);
