@@ -183,7 +183,7 @@ struct PCGArgs {
     const double* cva;
     const unsigned char* fixed;
     const int* diag_spos;
-    double *x, *r, *u, *w, *p, *s, *minv;
+    double *x, *r, *u, *w, *p, *s, *minv;   // u: stride 4 (padded); the others stride 3
     double* part;                    // [3][nblk]
     double* sc;                      // scalars, see SC_*
     int* flag;                       // [0] done, [1] iterations, [2] ticket
@@ -191,24 +191,62 @@ struct PCGArgs {
 enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
 constexpr int PCG_THREADS = 128;
 
-// w_i = sum_j A_ij v_j over the elastic (sliced-ELL) and contact (block-CSR) rows of vertex i
+// w_i = sum_j A_ij v_j over the elastic (sliced-ELL) and contact (block-CSR) rows of vertex i;
+// v is stored with stride ST doubles per vertex (ST = 4: 32-byte aligned, two vector loads)
+template <int ST>
+__device__ __forceinline__ void load_v(const double* __restrict__ v, int j, double& a, double& b, double& c) {
+    if (ST == 4) {
+        const double2 ab = __ldg(reinterpret_cast<const double2*>(v + 4 * (size_t)j));
+        a = ab.x;
+        b = ab.y;
+        c = __ldg(v + 4 * (size_t)j + 2);
+    } else {
+        a = __ldg(v + 3 * (size_t)j);
+        b = __ldg(v + 3 * (size_t)j + 1);
+        c = __ldg(v + 3 * (size_t)j + 2);
+    }
+}
+
+template <int ST>
 __device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double* __restrict__ v, double& y0, double& y1, double& y2) {
     y0 = y1 = y2 = 0.0;
     const int sl = i >> 5, lane = i & 31;
     const int base = a.soff[sl], len = a.rlen[i];
-    for (int k = 0; k < len; ++k) {
-        const size_t slot = (size_t)(base + k);
-        const int j = __ldg(a.scol + slot * 32 + lane);
-        const double* B = a.sval + slot * 288 + lane;
-        const double v0 = __ldg(v + 3 * j), v1 = __ldg(v + 3 * j + 1), v2 = __ldg(v + 3 * j + 2);
-        y0 += __ldg(B + 0) * v0 + __ldg(B + 32) * v1 + __ldg(B + 64) * v2;
-        y1 += __ldg(B + 96) * v0 + __ldg(B + 128) * v1 + __ldg(B + 160) * v2;
-        y2 += __ldg(B + 192) * v0 + __ldg(B + 224) * v1 + __ldg(B + 256) * v2;
+    int k = 0;
+    // two blocks per trip: their index, value and vector loads are independent
+    for (; k + 1 < len; k += 2) {
+        const size_t s0 = (size_t)(base + k), s1 = s0 + 1;
+        const int j0 = __ldg(a.scol + s0 * 32 + lane), j1 = __ldg(a.scol + s1 * 32 + lane);
+        const double* B = a.sval + s0 * 288 + lane;
+        const double* C = a.sval + s1 * 288 + lane;
+        double b[9], c[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            b[q] = __ldg(B + 32 * q);
+            c[q] = __ldg(C + 32 * q);
+        }
+        double p0, p1, p2, q0, q1, q2;
+        load_v<ST>(v, j0, p0, p1, p2);
+        load_v<ST>(v, j1, q0, q1, q2);
+        y0 += b[0] * p0 + b[1] * p1 + b[2] * p2 + c[0] * q0 + c[1] * q1 + c[2] * q2;
+        y1 += b[3] * p0 + b[4] * p1 + b[5] * p2 + c[3] * q0 + c[4] * q1 + c[5] * q2;
+        y2 += b[6] * p0 + b[7] * p1 + b[8] * p2 + c[6] * q0 + c[7] * q1 + c[8] * q2;
+    }
+    if (k < len) {
+        const size_t s0 = (size_t)(base + k);
+        const int j0 = __ldg(a.scol + s0 * 32 + lane);
+        const double* B = a.sval + s0 * 288 + lane;
+        double p0, p1, p2;
+        load_v<ST>(v, j0, p0, p1, p2);
+        y0 += __ldg(B + 0) * p0 + __ldg(B + 32) * p1 + __ldg(B + 64) * p2;
+        y1 += __ldg(B + 96) * p0 + __ldg(B + 128) * p1 + __ldg(B + 160) * p2;
+        y2 += __ldg(B + 192) * p0 + __ldg(B + 224) * p1 + __ldg(B + 256) * p2;
     }
     for (int e = a.crp[i]; e < a.crp[i + 1]; ++e) {
         const int j = a.cci[e];
         const double* B = a.cva + 9 * (size_t)e;
-        const double v0 = v[3 * j], v1 = v[3 * j + 1], v2 = v[3 * j + 2];
+        double v0, v1, v2;
+        load_v<ST>(v, j, v0, v1, v2);
         y0 += B[0] * v0 + B[1] * v1 + B[2] * v2;
         y1 += B[3] * v0 + B[4] * v1 + B[5] * v2;
         y2 += B[6] * v0 + B[7] * v1 + B[8] * v2;
@@ -299,16 +337,17 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const doub
         }
         for (int k = 0; k < 9; ++k) a.minv[9 * (size_t)i + k] = Mi[k];
         double y0, y1, y2;
-        row_apply(a, i, a.x, y0, y1, y2);
+        row_apply<3>(a, i, a.x, y0, y1, y2);
         const double r0 = fx ? 0.0 : rhs[3 * i] - y0, r1 = fx ? 0.0 : rhs[3 * i + 1] - y1, r2 = fx ? 0.0 : rhs[3 * i + 2] - y2;
         a.r[3 * i] = r0;
         a.r[3 * i + 1] = r1;
         a.r[3 * i + 2] = r2;
         for (int d = 0; d < 3; ++d) {
-            a.u[3 * i + d] = Mi[3 * d] * r0 + Mi[3 * d + 1] * r1 + Mi[3 * d + 2] * r2;
+            a.u[4 * i + d] = Mi[3 * d] * r0 + Mi[3 * d + 1] * r1 + Mi[3 * d + 2] * r2;
             a.p[3 * i + d] = 0.0;
             a.s[3 * i + d] = 0.0;
         }
+        a.u[4 * i + 3] = 0.0;
         rr = r0 * r0 + r1 * r1 + r2 * r2;
     }
     const double v[1] = {rr};
@@ -334,11 +373,11 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_spmv(PCGArgs a, int k) {
     double g = 0.0, dl = 0.0, rr = 0.0;
     if (i < a.nV) {
         double y0 = 0.0, y1 = 0.0, y2 = 0.0;
-        if (!a.fixed[i]) row_apply(a, i, a.u, y0, y1, y2);
+        if (!a.fixed[i]) row_apply<4>(a, i, a.u, y0, y1, y2);
         a.w[3 * i] = y0;
         a.w[3 * i + 1] = y1;
         a.w[3 * i + 2] = y2;
-        const double u0 = a.u[3 * i], u1 = a.u[3 * i + 1], u2 = a.u[3 * i + 2];
+        const double u0 = a.u[4 * i], u1 = a.u[4 * i + 1], u2 = a.u[4 * i + 2];
         const double r0 = a.r[3 * i], r1 = a.r[3 * i + 1], r2 = a.r[3 * i + 2];
         g = r0 * u0 + r1 * u1 + r2 * u2;
         dl = y0 * u0 + y1 * u1 + y2 * u2;
@@ -376,7 +415,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_update(PCGArgs a) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
         const int q = 3 * i + d;
-        const double p = a.u[q] + beta * a.p[q];
+        const double p = a.u[4 * i + d] + beta * a.p[q];
         const double s = a.w[q] + beta * a.s[q];
         a.p[q] = p;
         a.s[q] = s;
@@ -386,7 +425,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_update(PCGArgs a) {
     }
     const double* Mi = a.minv + 9 * (size_t)i;
 #pragma unroll
-    for (int d = 0; d < 3; ++d) a.u[3 * i + d] = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
+    for (int d = 0; d < 3; ++d) a.u[4 * i + d] = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
 }
 
 // ---------------------------------------------------------------- host side
@@ -499,7 +538,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
               cudaStream_t s) {
     const long long n3 = 3ll * c->nV;
     const int nb = nblk(c->nV, PCG_THREADS);
-    if (c->pcg_vec.ensure(8 * (n3 * 6 + 9ll * c->nV)) || c->pcg_part.ensure(8ll * (3 * nb + SC_COUNT) + 64) || c->scal.ensure(64))
+    if (c->pcg_vec.ensure(8 * (n3 * 4 + 13ll * c->nV) + 64) || c->pcg_part.ensure(8ll * (3 * nb + SC_COUNT) + 64) || c->scal.ensure(64))
         return FIPC_ERR_CUDA;
     if (c->c_nnzb == 0 && (c->c_rowptr.ensure(4ll * (c->nV + 1)) || cudaMemsetAsync(c->c_rowptr.p, 0, 4ll * (c->nV + 1), s)))
         return FIPC_ERR_CUDA;
@@ -517,12 +556,12 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     a.diag_spos = c->diag_spos;
     double* v = c->pcg_vec.as<double>();
     a.x = sol;
-    a.r = v;
-    a.u = v + n3;
-    a.w = v + 2 * n3;
-    a.p = v + 3 * n3;
-    a.s = v + 4 * n3;
-    a.minv = v + 5 * n3;
+    a.u = v;                       // 4 nV, first so that it is 32-byte aligned
+    a.r = v + 4ll * c->nV;
+    a.w = a.r + n3;
+    a.p = a.w + n3;
+    a.s = a.p + n3;
+    a.minv = a.s + n3;
     a.part = c->pcg_part.as<double>();
     a.sc = a.part + 3 * nb;
     a.flag = (int*)(c->scal.as<char>() + 48);
@@ -530,9 +569,9 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     // traffic model per launch: matrix blocks and column ids once (padding slots included),
     // row data, the gathered vector once, w written, r read
     const double slots = 32.0 * (double)c->n_slots, nv = (double)c->nV, cn = (double)c->c_nnzb;
-    const double spmv_bytes = slots * (72.0 + 4.0) + cn * 76.0 + nv * (4.0 + 4.0 + 1.0 + 24.0 + 24.0 + 24.0);
+    const double spmv_bytes = slots * (72.0 + 4.0) + cn * 76.0 + nv * (4.0 + 4.0 + 1.0 + 32.0 + 24.0 + 24.0);
     const double spmv_flops = (double)(c->nnzb + c->c_nnzb) * 18.0 + nv * 18.0;
-    const double upd_bytes = nv * (24.0 * 2 + 24.0 * 2 * 4 + 24.0 + 72.0);
+    const double upd_bytes = nv * (32.0 * 2 + 24.0 * 2 * 4 + 24.0 + 72.0);
     const double upd_flops = nv * 36.0;
     k_pcg_start<<<nb, PCG_THREADS, 0, s>>>(a, c->rhs, rtol);
     FIPC_LAUNCHED();
