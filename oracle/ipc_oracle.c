@@ -1423,11 +1423,22 @@ static double pdot(long long n, const double* a, const double* b) {
     return s;
 }
 
+int oracle_bsr_pcg_guess(int nV, const long long* rp, const int* ci, const double* va, const long long* crp, const int* cci,
+                         const double* cva, const long long* diag_pos, const double* b, const unsigned char* fixed, double rtol,
+                         int maxit, int use_guess, double* x);
+
 /* block-Jacobi PCG on elastic (rp, ci, va) + contact (crp, cci, cva) block-sparse matrices;
  * diag_pos: position of each diagonal block in the elastic matrix.  Returns iterations. */
 int oracle_bsr_pcg(int nV, const long long* rp, const int* ci, const double* va, const long long* crp, const int* cci,
                    const double* cva, const long long* diag_pos, const double* b, const unsigned char* fixed, double rtol, int maxit,
                    double* x) {
+    return oracle_bsr_pcg_guess(nV, rp, ci, va, crp, cci, cva, diag_pos, b, fixed, rtol, maxit, 0, x);
+}
+
+/* as oracle_bsr_pcg, starting from x when use_guess != 0; the tolerance is relative to |b| */
+int oracle_bsr_pcg_guess(int nV, const long long* rp, const int* ci, const double* va, const long long* crp, const int* cci,
+                         const double* cva, const long long* diag_pos, const double* b, const unsigned char* fixed, double rtol,
+                         int maxit, int use_guess, double* x) {
     const long long n = 3ll * nV;
     double *r = malloc(8 * n), *z = malloc(8 * n), *p = malloc(8 * n), *Ap = malloc(8 * n), *Mi = malloc(72 * (long long)nV);
     #pragma omp parallel for schedule(static)
@@ -1441,19 +1452,23 @@ int oracle_bsr_pcg(int nV, const long long* rp, const int* ci, const double* va,
         }
         inv3(B, Mi + 9 * i);
     }
+    double bb = 0;
+    for (int i = 0; i < nV; ++i)
+        for (int d = 0; d < 3; ++d) if (!fixed[i]) bb += b[3 * i + d] * b[3 * i + d];
+    if (!use_guess) memset(x, 0, sizeof(double) * (size_t)n);
+    for (int i = 0; i < nV; ++i) if (fixed[i]) x[3 * i] = x[3 * i + 1] = x[3 * i + 2] = 0;
+    bsr_spmv(nV, rp, ci, va, fixed, x, Ap, 0);
+    bsr_spmv(nV, crp, cci, cva, fixed, x, Ap, 1);
     #pragma omp parallel for schedule(static)
     for (int i = 0; i < nV; ++i)
-        for (int d = 0; d < 3; ++d) {
-            x[3 * i + d] = 0;
-            r[3 * i + d] = fixed[i] ? 0 : b[3 * i + d];
-        }
+        for (int d = 0; d < 3; ++d) r[3 * i + d] = fixed[i] ? 0 : b[3 * i + d] - Ap[3 * i + d];
     #pragma omp parallel for schedule(static)
     for (int i = 0; i < nV; ++i)
         for (int d = 0; d < 3; ++d) {
             z[3 * i + d] = Mi[9 * i + 3 * d] * r[3 * i] + Mi[9 * i + 3 * d + 1] * r[3 * i + 1] + Mi[9 * i + 3 * d + 2] * r[3 * i + 2];
             p[3 * i + d] = z[3 * i + d];
         }
-    double rz = pdot(n, r, z), rr0 = pdot(n, r, r);
+    double rz = pdot(n, r, z), rr0 = bb;
     int it = 0;
     for (; it < maxit; ++it) {
         const double rr = pdot(n, r, r);
