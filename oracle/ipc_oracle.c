@@ -1455,7 +1455,8 @@ int oracle_bsr_pcg_guess(int nV, const long long* rp, const int* ci, const doubl
     double bb = 0;
     for (int i = 0; i < nV; ++i)
         for (int d = 0; d < 3; ++d) if (!fixed[i]) bb += b[3 * i + d] * b[3 * i + d];
-    if (!use_guess) memset(x, 0, sizeof(double) * (size_t)n);
+    if (!use_guess)
+        for (long long i = 0; i < n; ++i) x[i] = 0.0;
     for (int i = 0; i < nV; ++i) if (fixed[i]) x[3 * i] = x[3 * i + 1] = x[3 * i + 2] = 0;
     bsr_spmv(nV, rp, ci, va, fixed, x, Ap, 0);
     bsr_spmv(nV, crp, cci, cva, fixed, x, Ap, 1);
