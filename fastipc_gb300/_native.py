@@ -22,6 +22,7 @@ EXPORTS = [
     'fipc_compute_hessian_and_gradient', 'fipc_system_sizes', 'fipc_export_system', 'fipc_solve_system',
     'fipc_output_residual', 'fipc_compute_energy', 'fipc_compute_intersection_free_step_size', 'fipc_check_collision',
     'fipc_launch_count', 'fipc_status_string', 'fipc_profile_enable', 'fipc_profile_read',
+    'fipc_compute_energy_noalloc',
 ]
 
 

@@ -96,6 +96,21 @@ int fipc_output_residual(fipc_ctx* ctx, const double* sol, double* res_h, void* 
 /* compute_energy, NEWTON_IPC.py:514-542, over the lists of the last find_constraints */
 int fipc_compute_energy(fipc_ctx* ctx, const double* x, const double* xtilde, double* e_h, void* stream);
 
+/* Allocation-free compute_energy for callers that cannot allocate device memory while running
+ * (a host application that reserves all device memory in one arena at start-up and forbids
+ * cudaMalloc afterwards, since it synchronises the device and can fail against the arena).  No
+ * counterpart in the reference.  Stateless: the caller passes mass [V], tets [T][4], dm_inv
+ * [T][9], vol/lam/mu [T], counts_h [7] (host) and rows_h [7] (host array of device row
+ * pointers), and receives the total in *energy (device).  The reduction's partial sums live in a
+ * fixed file-scope device array of 65,536 doubles (512 KiB per GPU that loads the library, held
+ * until exit): one partial per 256 vertices, tets or rows, so requests needing more (about 16.7M
+ * elements in total) return status 1.  The first call on a device looks up that array and must
+ * come before any stream capture; calls that overlap on the GPU share the array and race. */
+int fipc_compute_energy_noalloc(int n_verts, const double* x, const double* xtilde, const double* mass, int n_tets,
+                                const int* tets, const double* dm_inv, const double* vol, const double* lam,
+                                const double* mu, double dt, const int* counts_h, const int* const* rows_h,
+                                const double* x0, double dhat2, double kappa, double* energy, void* stream);
+
 /* compute_intersection_free_step_size, NEWTON_IPC.py:456-468 (PT :377-406, EE :409-440,
  * inversion :443-453 when `inversion` is nonzero) */
 int fipc_compute_intersection_free_step_size(fipc_ctx* ctx, const double* x, const double* p, double eta, int inversion,
