@@ -40,9 +40,13 @@ def parse():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--nx', type=int, default=400, help='hexes along the bar (400 = the 960k-tet configuration)')
     ap.add_argument('--pcg-rtol', type=float, default=1e-6)
+    ap.add_argument('--warm-start', type=int, default=1, help='PCG initial guess from the previous step (1) or zero (0)')
     ap.add_argument('--profile-kernel', type=int, default=1, help='kernel timed for the roofline (1 = PCG SpMV)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--cpu-sample-pcg', type=int, default=100000)
+    ap.add_argument('--workload', default='bar', choices=['bar', 'batch'],
+                    help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context')
+    ap.add_argument('--scenes', type=int, default=512, help='scenes of the batch workload')
     return ap.parse_args()
 
 
@@ -54,6 +58,7 @@ def make_scene(nx):
 def workload(nx, pcg_rtol):
     return {'workload': f'twisted bar {nx}x20x20 hexes x6 tets ({nx * 2400} tets), NH E=1e6 nu=0.45, dhat=5e-4, dt=0.01',
             'tets': nx * 2400, 'verts': (nx + 1) * 441, 'newton_tol': '|p|inf < 1e-2 dt', 'pcg_rtol': pcg_rtol,
+            'pcg_tolerance': 'relative to |rhs| on free DOFs',
             'l2': 'inputs larger than L2 (element Hessians alone ~0.7 GB per Newton iteration)'}
 
 
@@ -188,6 +193,8 @@ def run_reference(args):
 
 def main():
     args = parse()
+    if args.workload == 'batch':
+        return main_batch(args)
     if args.impl == 'reference':
         return run_reference(args)
     import numpy as np
@@ -207,7 +214,7 @@ def main():
     dev = torch.device('cuda', local)
     build()
     scene = make_scene(args.nx)
-    sim = NewtonIPC(scene, device=dev, pcg_rtol=args.pcg_rtol)
+    sim = NewtonIPC(scene, device=dev, pcg_rtol=args.pcg_rtol, pcg_warm_start=bool(args.warm_start))
 
     def barrier():
         if dist is not None:
@@ -219,6 +226,7 @@ def main():
         sim.step(f)
         f += 1
     snap = (sim.x.clone(), sim.v.clone())
+    hist = {k: v.clone() for k, v in sim._dir_hist.items()}
     f0 = f
     n_newton0, n_pcg0 = len(sim.newton_iters), len(sim.pcg_iters)
     L = _native.lib()
@@ -253,6 +261,7 @@ def main():
     hx.copy_(snap[0])
     hv.copy_(snap[1])
     sim.newton_iters, sim.pcg_iters = [], []
+    sim._dir_hist = {k: v.clone() for k, v in hist.items()}
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -302,6 +311,124 @@ def main():
     sim.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+BATCH_METRIC = 'scene-steps/s (cube stacks, batched)'
+
+
+def batch_workload(n):
+    return {'workload': f'{n} independent cube stacks (1-8 cubes of 3-10 hexes per side x6 tets over a fixed ground box, '
+                        f'seeds 0..{n - 1}), NH E=1e5 nu=0.4, dhat=1e-3, dt=0.01, one batch context',
+            'scenes': n, 'newton_tol': '|p|inf < 1e-2 dt per scene', 'l2': 'inputs larger than L2'}
+
+
+def main_batch(args):
+    """Batched scenes: W warm-up steps, K timed steps of all scenes (CUDA events), value =
+    scenes * K / time; the oracle steps a sample of the same scenes on the host cores."""
+    rank = int(os.environ.get('RANK', '0'))
+    from fastipc_gb300 import scenes as SC
+    scs = SC.cube_stacks(args.scenes, seed=0)
+    n_tets = sum(s.n_tets for s in scs)
+    cfg = batch_workload(args.scenes)
+    cfg.update({'tets': n_tets, 'verts': sum(s.n_verts for s in scs), 'pcg_rtol': args.pcg_rtol})
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        v, sample, cores = batch_cpu(scs, args)
+        print(json.dumps({'impl': 'reference', 'metric': BATCH_METRIC, 'value': v, 'unit': 'scene-steps/s', 'n_gpus': args.gpus,
+                          'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True, 'scaling': 'weak',
+                          'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
+                          'cpu_baseline': {'value': v, 'unit': 'scene-steps/s', 'cores': cores, 'kind': 'port', 'sample': sample},
+                          'e2e': {'value': v, 'unit': 'scene-steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}),
+              flush=True)
+        return
+    import torch
+    from fastipc_gb300 import _native
+    from fastipc_gb300.batch import BatchNewtonIPC
+    from fastipc_gb300.build import build
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    build()
+    t0 = time.perf_counter()
+    sim = BatchNewtonIPC(scs, device=dev, pcg_rtol=args.pcg_rtol)
+    t_setup = time.perf_counter() - t0
+    f = 0
+    for _ in range(args.warmup):
+        sim.step(f)
+        f += 1
+    snap = (sim.x.clone(), sim.v.clone())
+    f0 = f
+    n0 = len(sim.newton_iters)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _native.launch_count()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.step(f)
+            f += 1
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = _native.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    its = sim.newton_iters[n0:]
+    newton_rounds = sum(int(i.max()) for i in its)
+    # e2e: the same steps from the same state with the state round-tripped through pinned host memory
+    hx = torch.empty_like(snap[0], device='cpu').pin_memory()
+    hv = torch.empty_like(snap[1], device='cpu').pin_memory()
+    hx.copy_(snap[0])
+    hv.copy_(snap[1])
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    f = f0
+    for _ in range(args.steps):
+        sim.x.copy_(hx, non_blocking=True)
+        sim.v.copy_(hv, non_blocking=True)
+        sim.step(f)
+        hx.copy_(sim.x, non_blocking=True)
+        hv.copy_(sim.v, non_blocking=True)
+        f += 1
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1)
+    nbytes = 2 * sim.x.numel() * 8
+    out = {'metric': BATCH_METRIC, 'value': args.scenes * args.steps / (ms / 1e3), 'unit': 'scene-steps/s', 'n_gpus': 1,
+           'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': ms / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
+           'newton_iters_per_scene_step': float(sum(i.mean() for i in its) / len(its)),
+           'batched_newton_rounds_per_step': newton_rounds / len(its), 'ms_per_batched_newton_round': ms / max(newton_rounds, 1),
+           'pcg_shape': sim.pcg_shape(), 'setup_s': t_setup,
+           'e2e': {'value': args.scenes * args.steps / (e2e_ms / 1e3), 'unit': 'scene-steps/s', 'h2d_bytes_per_step': nbytes,
+                   'd2h_bytes_per_step': nbytes},
+           'gpu_launches': launches, 'clocks': clk.summary(), 'sections_s': {k: round(v, 4) for k, v in sim.timer.total.items()}}
+    if not args.no_cpu_baseline:
+        v, sample, cores = batch_cpu(scs, args)
+        out['cpu_baseline'] = {'value': v, 'unit': 'scene-steps/s', 'cores': cores, 'kind': 'port', 'sample': sample}
+    print(json.dumps(out), flush=True)
+    sim.close()
+
+
+def batch_cpu(scs, args, budget_s=20.0):
+    """The oracle steps scenes of the batch (every 16th, after the same warm-up) one at a time
+    on the host cores until about budget_s of stepping; scene-steps/s of that sample."""
+    from oracle import oracle as O
+    done, t_total, names = 0, 0.0, []
+    for k in range(0, len(scs), 16):
+        sim = O.OracleSim(scs[k], solver='bsr', pcg_rtol=args.pcg_rtol, pcg_maxit=args.cpu_sample_pcg)
+        for f in range(args.warmup):
+            sim.step(f)
+        t0 = time.perf_counter()
+        sim.step(args.warmup)
+        t_total += time.perf_counter() - t0
+        done += 1
+        names.append(k)
+        if t_total > budget_s:
+            break
+    sample = f'one time step (step {args.warmup}) of scenes {names} stepped one at a time, {t_total:.1f} s'
+    return done / t_total, sample, O.lib().oracle_num_threads()
 
 
 def ctypes_read(L):

@@ -27,6 +27,13 @@ __device__ __forceinline__ C3 cell_of(v3 p, double inv_dx) {
     return C3{(long long)floor(p.x * inv_dx), (long long)floor(p.y * inv_dx), (long long)floor(p.z * inv_dx)};
 }
 __device__ __forceinline__ C3 cmax(C3 a, C3 b) { return C3{a.x > b.x ? a.x : b.x, a.y > b.y ? a.y : b.y, a.z > b.z ? a.z : b.z}; }
+__device__ __forceinline__ unsigned long long gkey(const SceneGeo& g, int s, long long cx, long long cy, long long cz) {
+    return g.vscene ? cell_key_scene(s, cx, cy, cz) : cell_key(cx, cy, cz);
+}
+// first vertex of stored primitive i (its scene)
+__device__ __forceinline__ int prim_vertex(int mode, int i, const int* __restrict__ prim) {
+    return (mode == 0 || mode == 2) ? prim[i] : prim[2 * i];
+}
 
 // Box modes of stored primitives:
 //  0 point [p - dh, p + dh]               (find constraints, point-triangle)
@@ -66,10 +73,11 @@ __device__ __forceinline__ void stored_box(int mode, int i, const int* __restric
 constexpr long long MAX_CELLS_PER_PRIM = 1ll << 22;
 
 __global__ void k_cell_count(int mode, int n, const int* __restrict__ prim, const double* __restrict__ x,
-                             const double* __restrict__ p, double dh, double inv_dx, long long* __restrict__ cnt,
+                             const double* __restrict__ p, double dh, SceneGeo g, long long* __restrict__ cnt,
                              int* __restrict__ overflow) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    const double inv_dx = g.idx(g.scene(prim_vertex(mode, i, prim)));
     v3 lo, hi;
     stored_box(mode, i, prim, x, p, dh, &lo, &hi);
     const C3 a = cell_of(lo, inv_dx), b = cell_of(hi, inv_dx);
@@ -82,10 +90,12 @@ __global__ void k_cell_count(int mode, int n, const int* __restrict__ prim, cons
 }
 
 __global__ void k_cell_emit(int mode, int n, const int* __restrict__ prim, const double* __restrict__ x,
-                            const double* __restrict__ p, double dh, double inv_dx, const long long* __restrict__ off,
+                            const double* __restrict__ p, double dh, SceneGeo g, const long long* __restrict__ off,
                             const long long* __restrict__ cnt, unsigned long long* __restrict__ keys, int* __restrict__ ids) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n || cnt[i] == 0) return;
+    const int sc = g.scene(prim_vertex(mode, i, prim));
+    const double inv_dx = g.idx(sc);
     v3 lo, hi;
     stored_box(mode, i, prim, x, p, dh, &lo, &hi);
     const C3 a = cell_of(lo, inv_dx), b = cell_of(hi, inv_dx);
@@ -93,7 +103,7 @@ __global__ void k_cell_emit(int mode, int n, const int* __restrict__ prim, const
     for (long long cx = a.x; cx <= b.x; ++cx)
         for (long long cy = a.y; cy <= b.y; ++cy)
             for (long long cz = a.z; cz <= b.z; ++cz) {
-                keys[o] = cell_key(cx, cy, cz);
+                keys[o] = gkey(g, sc, cx, cy, cz);
                 ids[o] = i;
                 ++o;
             }
@@ -162,19 +172,21 @@ __device__ void attempt_ee(const double* __restrict__ x, const double* __restric
 
 // one thread per boundary triangle; points hashed with mode 0
 __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
-                                                 const double* __restrict__ x, double dh, double dh2, double inv_dx,
+                                                 const double* __restrict__ x, double dh, double dh2, SceneGeo g,
                                                  const unsigned long long* __restrict__ uk, const int* __restrict__ us,
                                                  const int* __restrict__ nu_p, const int* __restrict__ ids, RowSink sink) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     const int nu = *nu_p;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
+    const int sc = g.scene(t0);
+    const double inv_dx = g.idx(sc);
     const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
     const C3 lo = cell_of(vmin(vmin(A, B), C), inv_dx), hi = cell_of(vmax(vmax(A, B), C), inv_dx);
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
                 for (int k = us[c]; k < us[c + 1]; ++k) {
                     const int j = ids[k];
@@ -189,20 +201,22 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
 
 // one thread per boundary edge (query, box +- dh); stored edges hashed with mode 1
 __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
-                                                 const double* __restrict__ x0, double dh, double dh2, double inv_dx,
+                                                 const double* __restrict__ x0, double dh, double dh2, SceneGeo g,
                                                  const unsigned long long* __restrict__ uk, const int* __restrict__ us,
                                                  const int* __restrict__ nu_p, const int* __restrict__ ids, RowSink sink) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbe) return;
     const int nu = *nu_p;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
+    const int sc = g.scene(a0);
+    const double inv_dx = g.idx(sc);
     const v3 A0 = ld3(x, a0), A1 = ld3(x, a1);
     const v3 d = mk(dh, dh, dh);
     const C3 lo = cell_of(vmin(A0, A1) - d, inv_dx), hi = cell_of(vmax(A0, A1) + d, inv_dx);
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
                 for (int k = us[c]; k < us[c + 1]; ++k) {
                     const int j = ids[k];
@@ -223,7 +237,7 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* slot, double 
 
 // compute_filter_3D_PT (NEWTON_IPC.py:377-406): triangles query their moving bbox
 __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
-                                                const double* __restrict__ x, const double* __restrict__ p, double dh, double inv_dx,
+                                                const double* __restrict__ x, const double* __restrict__ p, double dh, SceneGeo g,
                                                 double eta, const unsigned long long* __restrict__ uk, const int* __restrict__ us,
                                                 const int* __restrict__ nu_p, const int* __restrict__ ids,
                                                 unsigned long long* __restrict__ alpha) {
@@ -231,6 +245,8 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
     if (i >= nbt) return;
     const int nu = *nu_p;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
+    const int sc = g.scene(t0);
+    const double inv_dx = g.idx(sc);
     const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
     const v3 dA = ld3(p, t0), dB = ld3(p, t1), dC = ld3(p, t2);
     const v3 mn = vmin(vmin(vmin(A, A + dA), vmin(B, B + dB)), vmin(C, C + dC));
@@ -240,7 +256,7 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
                 for (int k = us[c]; k < us[c + 1]; ++k) {
                     const int pp = bp[ids[k]];
@@ -251,14 +267,14 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
                     if (first.x != cx || first.y != cy || first.z != cz) continue;
                     if (!pt_aabb_moving(P, A, B, C, dP, dA, dB, dC, dh)) continue;
                     const double d2 = pt_dist2(P, A, B, C);
-                    atomic_min_pos(alpha, pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, d2));
+                    atomic_min_pos(alpha + (g.vscene ? sc : 0), pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, d2));
                 }
             }
 }
 
 // compute_filter_3D_EE (NEWTON_IPC.py:409-440): edges query moving bbox +- dh
 __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
-                                                const double* __restrict__ p, double dh, double inv_dx, double eta,
+                                                const double* __restrict__ p, double dh, SceneGeo g, double eta,
                                                 const unsigned long long* __restrict__ uk, const int* __restrict__ us,
                                                 const int* __restrict__ nu_p, const int* __restrict__ ids,
                                                 unsigned long long* __restrict__ alpha) {
@@ -266,6 +282,8 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
     if (i >= nbe) return;
     const int nu = *nu_p;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
+    const int sc = g.scene(a0);
+    const double inv_dx = g.idx(sc);
     const v3 A0 = ld3(x, a0), A1 = ld3(x, a1), dA0 = ld3(p, a0), dA1 = ld3(p, a1);
     const v3 d = mk(dh, dh, dh);
     const v3 mn = vmin(vmin(A0, A0 + dA0), vmin(A1, A1 + dA1)), mx = vmax(vmax(A0, A0 + dA0), vmax(A1, A1 + dA1));
@@ -273,7 +291,7 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
                 for (int k = us[c]; k < us[c + 1]; ++k) {
                     const int j = ids[k];
@@ -286,39 +304,43 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
                     if (first.x != cx || first.y != cy || first.z != cz) continue;
                     if (!ee_aabb_moving(A0, A1, B0, B1, dA0, dA1, dB0, dB1, dh)) continue;
                     const double d2 = ee_dist2(A0, A1, B0, B1);
-                    atomic_min_pos(alpha, ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2));
+                    atomic_min_pos(alpha + (g.vscene ? sc : 0), ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2));
                 }
             }
 }
 
 // compute_filter_3D_inversion_free (NEWTON_IPC.py:443-453)
 __global__ void __launch_bounds__(128) k_ccd_inversion(int nT, const int4* __restrict__ tets, const double* __restrict__ x,
-                                                       const double* __restrict__ p, double eta, unsigned long long* __restrict__ alpha) {
+                                                       const double* __restrict__ p, double eta, SceneGeo g,
+                                                       unsigned long long* __restrict__ alpha) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= nT) return;
     const int4 t = tets[e];
     const v3 X[4] = {ld3(x, t.x), ld3(x, t.y), ld3(x, t.z), ld3(x, t.w)};
     const v3 P[4] = {ld3(p, t.x), ld3(p, t.y), ld3(p, t.z), ld3(p, t.w)};
-    atomic_min_pos(alpha, inversion_free_step(X, P, eta));
+    atomic_min_pos(alpha + (g.vscene ? g.scene(t.x) : 0), inversion_free_step(X, P, eta));
 }
 
 // check_collision_3d (NEWTON_IPC.py:855-880): triangles query bbox cells, edges hashed +- dh
 __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restrict__ bt, const int* __restrict__ be,
-                                                   const double* __restrict__ x, double dh, double inv_dx,
+                                                   const double* __restrict__ x, double dh, SceneGeo g,
                                                    const unsigned long long* __restrict__ uk, const int* __restrict__ us,
                                                    const int* __restrict__ nu_p, const int* __restrict__ ids, int* __restrict__ hit) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     const int nu = *nu_p;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
+    const int sc = g.scene(t0);
+    const double inv_dx = g.idx(sc);
     const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
     const C3 lo = cell_of(vmin(vmin(A, B), C), inv_dx), hi = cell_of(vmax(vmax(A, B), C), inv_dx);
     const v3 d = mk(dh, dh, dh);
+    hit += g.vscene ? sc : 0;
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
                 if (*(volatile int*)hit) return;
-                const int c = find_cell(uk, nu, cell_key(cx, cy, cz));
+                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
                 for (int k = us[c]; k < us[c + 1]; ++k) {
                     const int j = ids[k];
@@ -386,6 +408,14 @@ static int cub_call(fipc_ctx* c, F&& f) {
     return FIPC_OK;
 }
 
+static SceneGeo geo(const fipc_ctx* c) {
+    SceneGeo g;
+    g.vscene = c->n_scenes > 1 ? c->v_scene : nullptr;
+    g.inv_dx_s = c->s_inv_dx;
+    g.inv_dx = c->inv_dx;
+    return g;
+}
+
 // build grid g over n stored primitives; scal: device int scratch (overflow flag at [0])
 int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const double* x, const double* p, cudaStream_t s) {
     g.n_entries = 0;
@@ -396,7 +426,7 @@ int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const dou
     FIPC_CUDA(cudaMemsetAsync(g.ncells.p, 0, sizeof(int) * 2, s));
     if (n == 0) return FIPC_OK;
     int* ovf = g.ncells.as<int>() + 1;
-    k_cell_count<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, c->inv_dx, g.counts.as<long long>(), ovf);
+    k_cell_count<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, geo(c), g.counts.as<long long>(), ovf);
     FIPC_LAUNCHED();
     long long* cnt = g.counts.as<long long>();
     long long* off = g.offsets.as<long long>();
@@ -416,7 +446,7 @@ int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const dou
     if (g.keys.ensure(8 * total) || g.keys_alt.ensure(8 * total) || g.ids.ensure(4 * total) || g.ids_alt.ensure(4 * total) ||
         g.ukeys.ensure(8 * total) || g.ustart.ensure(4 * (total + 1)) || g.tmp.ensure(4 * (total + 1)))
         return FIPC_ERR_CUDA;
-    k_cell_emit<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, c->inv_dx, off, cnt, g.keys.as<unsigned long long>(),
+    k_cell_emit<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, geo(c), off, cnt, g.keys.as<unsigned long long>(),
                                              g.ids.as<int>());
     FIPC_LAUNCHED();
     cub::DoubleBuffer<unsigned long long> kb(g.keys.as<unsigned long long>(), g.keys_alt.as<unsigned long long>());
@@ -508,7 +538,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         int st = build_grid(c, c->gp, 0, c->nBP, c->bp, x, nullptr, s);
         if (st) return st;
         if (c->gp.n_entries > 0 && c->nBT > 0) {
-            k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, c->inv_dx,
+            k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, geo(c),
                                                          c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
                                                          c->gp.ncells.as<int>(), c->gp.ids.as<int>(), sink);
             FIPC_LAUNCHED();
@@ -516,7 +546,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         st = build_grid(c, c->ge, 1, c->nBE, c->be, x, nullptr, s);
         if (st) return st;
         if (c->ge.n_entries > 0) {
-            k_find_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, c->inv_dx,
+            k_find_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, geo(c),
                                                          c->ge.ukeys.as<unsigned long long>(), c->ge.ustart.as<int>(),
                                                          c->ge.ncells.as<int>(), c->ge.ids.as<int>(), sink);
             FIPC_LAUNCHED();
@@ -536,16 +566,13 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
     return FIPC_ERR_CAPACITY;
 }
 
-// compute_intersection_free_step_size (NEWTON_IPC.py:456-468); result in *alpha_h
-int ccd_step(fipc_ctx* c, const double* x, const double* p, double eta, bool inversion, double* alpha_h, cudaStream_t s) {
-    if (c->scal.ensure(64)) return FIPC_ERR_CUDA;
-    unsigned long long* slot = c->scal.as<unsigned long long>();
-    const double one = 1.0;
-    FIPC_CUDA(cudaMemcpyAsync(slot, &one, 8, cudaMemcpyHostToDevice, s));
+// compute_intersection_free_step_size (NEWTON_IPC.py:456-468): the launches, min'd into
+// slots (one double per scene, preset to 1.0 by the caller)
+int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool inversion, unsigned long long* slot, cudaStream_t s) {
     int st = build_grid(c, c->gp, 2, c->nBP, c->bp, x, p, s);
     if (st) return st;
     if (c->gp.n_entries > 0 && c->nBT > 0) {
-        k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, c->inv_dx, eta,
+        k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, geo(c), eta,
                                                     c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
                                                     c->gp.ncells.as<int>(), c->gp.ids.as<int>(), slot);
         FIPC_LAUNCHED();
@@ -553,17 +580,42 @@ int ccd_step(fipc_ctx* c, const double* x, const double* p, double eta, bool inv
     st = build_grid(c, c->ge, 3, c->nBE, c->be, x, p, s);
     if (st) return st;
     if (c->ge.n_entries > 0) {
-        k_ccd_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, c->inv_dx, eta, c->ge.ukeys.as<unsigned long long>(),
+        k_ccd_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, geo(c), eta, c->ge.ukeys.as<unsigned long long>(),
                                                     c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), slot);
         FIPC_LAUNCHED();
     }
     if (inversion && c->nT > 0) {
-        k_ccd_inversion<<<nblk(c->nT, 128), 128, 0, s>>>(c->nT, (const int4*)c->tets, x, p, eta, slot);
+        k_ccd_inversion<<<nblk(c->nT, 128), 128, 0, s>>>(c->nT, (const int4*)c->tets, x, p, eta, geo(c), slot);
         FIPC_LAUNCHED();
     }
     FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+
+// one scene: result in *alpha_h
+int ccd_step(fipc_ctx* c, const double* x, const double* p, double eta, bool inversion, double* alpha_h, cudaStream_t s) {
+    if (c->scal.ensure(64)) return FIPC_ERR_CUDA;
+    unsigned long long* slot = c->scal.as<unsigned long long>();
+    const double one = 1.0;
+    FIPC_CUDA(cudaMemcpyAsync(slot, &one, 8, cudaMemcpyHostToDevice, s));
+    int st = ccd_launch(c, x, p, eta, inversion, slot, s);
+    if (st) return st;
     FIPC_CUDA(cudaMemcpyAsync(alpha_h, slot, 8, cudaMemcpyDeviceToHost, s));
     FIPC_CUDA(cudaStreamSynchronize(s));
+    return FIPC_OK;
+}
+
+// check_collision_3d (NEWTON_IPC.py:881-886): the launches, or'd into hit (one int per scene,
+// zeroed by the caller)
+int collision_launch(fipc_ctx* c, const double* x, int* hit, cudaStream_t s) {
+    int st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, s);
+    if (st) return st;
+    if (c->ge.n_entries > 0 && c->nBT > 0) {
+        k_collision<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, geo(c), c->ge.ukeys.as<unsigned long long>(),
+                                                       c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), hit);
+        FIPC_LAUNCHED();
+    }
+    FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
 }
 
@@ -571,14 +623,8 @@ int check_collision(fipc_ctx* c, const double* x, int* hit_h, cudaStream_t s) {
     if (c->scal.ensure(64)) return FIPC_ERR_CUDA;
     int* hit = (int*)(c->scal.as<char>() + 16);
     FIPC_CUDA(cudaMemsetAsync(hit, 0, sizeof(int), s));
-    int st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, s);
+    int st = collision_launch(c, x, hit, s);
     if (st) return st;
-    if (c->ge.n_entries > 0 && c->nBT > 0) {
-        k_collision<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, c->inv_dx, c->ge.ukeys.as<unsigned long long>(),
-                                                       c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), hit);
-        FIPC_LAUNCHED();
-    }
-    FIPC_CUDA(cudaGetLastError());
     FIPC_CUDA(cudaMemcpyAsync(hit_h, hit, sizeof(int), cudaMemcpyDeviceToHost, s));
     FIPC_CUDA(cudaStreamSynchronize(s));
     return FIPC_OK;

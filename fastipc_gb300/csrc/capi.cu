@@ -24,6 +24,7 @@ int sell_to_bsr(fipc_ctx* c, double* out, cudaStream_t s);
 int launch_energy(const fipc_ctx* c, const double* x, const double* xt, const int* const* rows, const int* counts, double* part,
                   double* out, cudaStream_t s);
 int launch_absmax(int n, const double* p, double* part, double* out, cudaStream_t s);
+void free_batch(fipc_ctx* c);
 }  // namespace fipc
 
 using namespace fipc;
@@ -44,6 +45,7 @@ double det3h(const double* A) {
 }
 
 void free_ctx(fipc_ctx* c) {
+    free_batch(c);
     void* ptrs[] = {c->tets, c->bp, c->be, c->bt, c->dminv, c->vol, c->lam, c->mu, c->mass, c->x0, c->row_ptr, c->col_idx,
                     c->up_pos, c->up_tpos, c->up_row, c->up_cptr, c->up_contrib, c->vt_ptr, c->vt_list, c->elem_g, c->elem_H,
                     c->bsr_val, c->rhs, c->d_counts, c->diag_pos, c->sell_off, c->sell_col, c->row_len, c->bsr2sell,
@@ -53,7 +55,7 @@ void free_ctx(fipc_ctx* c) {
     for (int t = 0; t < N_TYPES; ++t) c->rows[t].release();
     DBuf* bufs[] = {&c->rows_tmp, &c->sort_keys, &c->sort_keys_alt, &c->sort_vals, &c->sort_vals_alt, &c->flags, &c->scan,
                     &c->cub_tmp, &c->c_g, &c->c_H, &c->c_keys, &c->c_keys_alt, &c->c_vals, &c->c_vals_alt, &c->c_ukeys,
-                    &c->c_ucount, &c->c_ustart, &c->c_val, &c->c_rowptr, &c->c_col, &c->pcg_vec, &c->pcg_part, &c->scal, &c->red};
+                    &c->c_ucount, &c->c_ustart, &c->c_val, &c->c_rowptr, &c->c_col, &c->pcg_vec, &c->pcg_part, &c->scal, &c->red, &c->mlp_dist};
     for (DBuf* b : bufs) b->release();
     Grid* gs[] = {&c->gp, &c->ge};
     for (Grid* g : gs) {

@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include <atomic>
+#include <vector>
 
 #include "common.cuh"
 
@@ -93,6 +94,34 @@ struct fipc_ctx_impl {
     Grid gp, ge;
     // small device scalars: [0] alpha bits, [1] hit flag, reductions ...
     DBuf scal, red;
+    // learned warm start: per-vertex nearest-constraint distance
+    DBuf mlp_dist;
+    // batched scenes (n_scenes > 1): scene s owns vertices [voff[s], voff[s+1]) and tets
+    // [toff[s], toff[s+1]); its own kappa and hash cell; null tables for a single scene
+    int n_scenes = 1;
+    int *v_scene = nullptr, *voff_d = nullptr, *toff_d = nullptr;
+    double *s_kappa = nullptr, *s_inv_dx = nullptr;
+    std::vector<int> h_voff, h_toff;
+    std::vector<double> h_kappa, h_inv_dx;
+    // batched PCG: tiles of consecutive rows inside one scene
+    int n_tiles = 0, tile_rows = 0, pcg_grid = 0;
+    DBuf tile_scene, tile_row0, scene_tile0, bpcg_vec, bpcg_sc, bpcg_part, bpcg_flag, s_red, s_rowoff;
+    void* graph_exec = nullptr;           // captured PCG chunk (cudaGraphExec_t)
+    void* cap_stream = nullptr;           // private stream used only for capturing it
+    std::vector<unsigned char> graph_sig; // the kernel arguments it was captured with
+    float tune_ms = 0.f;                  // time of one SpMV launch in the chosen shape
+};
+
+// scene lookup for the spatial hash: one scene (null table) or per-vertex scene ids with
+// per-scene cell sizes; keys of different scenes never coincide
+struct SceneGeo {
+    const int* vscene = nullptr;
+    const double* inv_dx_s = nullptr;
+    double inv_dx = 1.0;
+#if defined(__CUDACC__)
+    __device__ __forceinline__ int scene(int v) const { return vscene ? __ldg(vscene + v) : 0; }
+    __device__ __forceinline__ double idx(int s) const { return vscene ? __ldg(inv_dx_s + s) : inv_dx; }
+#endif
 };
 
 // ---------------------------------------------------------------- shared device helpers
@@ -110,6 +139,13 @@ FIPC_HD unsigned long long cell_key(long long i, long long j, long long k) {
     const long long off = 1ll << 20;
     auto c = [](long long v) { return v < 0 ? 0ll : (v > (1ll << 21) - 1 ? (1ll << 21) - 1 : v); };
     return ((unsigned long long)c(i + off) << 42) | ((unsigned long long)c(j + off) << 21) | (unsigned long long)c(k + off);
+}
+// batched scenes: 10 bits of scene id above 18 bits per axis (offset 2^17)
+FIPC_HD unsigned long long cell_key_scene(int s, long long i, long long j, long long k) {
+    const long long off = 1ll << 17;
+    auto c = [](long long v) { return v < 0 ? 0ll : (v > (1ll << 18) - 1 ? (1ll << 18) - 1 : v); };
+    return ((unsigned long long)s << 54) | ((unsigned long long)c(i + off) << 36) | ((unsigned long long)c(j + off) << 18) |
+           (unsigned long long)c(k + off);
 }
 
 }  // namespace fipc

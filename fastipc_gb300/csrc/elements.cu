@@ -41,11 +41,13 @@ __global__ void __launch_bounds__(128) k_elasticity(int nT, const int4* __restri
 // (v*4+w, nv x nv used) of the projected barrier Hessian (common/math/ipc.py *_g_and_H).
 __global__ void __launch_bounds__(128) k_barrier_rows(int type, int n, const int4* __restrict__ rows,
                                                       const double* __restrict__ x, const double* __restrict__ x0, double dh2,
-                                                      double kappa, double* __restrict__ E, double* __restrict__ g,
-                                                      double* __restrict__ Hb, int* __restrict__ status) {
+                                                      double kappa, const double* __restrict__ kap_s, const int* __restrict__ vscene,
+                                                      double* __restrict__ E, double* __restrict__ g, double* __restrict__ Hb,
+                                                      int* __restrict__ status) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= n) return;
     const int4 q = rows[r];
+    if (kap_s) kappa = kap_s[vscene[q.x]];   // batched scenes: the row's own scene
     const int nv = type_nverts(type);
     const int id[4] = {q.x, q.y, nv > 2 ? q.z : q.x, nv > 3 ? q.w : q.x};
     v3 X[4], X0[4];
@@ -115,12 +117,14 @@ __global__ void __launch_bounds__(RED_THREADS) k_energy_elastic(int nT, const in
 // barrier energies of one list (NEWTON_IPC.py:527-541)
 __global__ void __launch_bounds__(RED_THREADS) k_energy_barrier(int type, int n, const int4* __restrict__ rows,
                                                                 const double* __restrict__ x, const double* __restrict__ x0,
-                                                                double dh2, double kappa, double* __restrict__ part) {
+                                                                double dh2, double kappa, const double* __restrict__ kap_s,
+                                                                const int* __restrict__ vscene, double* __restrict__ part) {
     __shared__ double sh[RED_THREADS];
     double acc = 0.0;
     const int nv = type_nverts(type);
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
         const int4 q = rows[r];
+        const double kap = kap_s ? kap_s[vscene[q.x]] : kappa;
         const int id[4] = {q.x, q.y, nv > 2 ? q.z : q.x, nv > 3 ? q.w : q.x};
         v3 X[4], X0[4];
         for (int k = 0; k < 4; ++k) {
@@ -128,7 +132,7 @@ __global__ void __launch_bounds__(RED_THREADS) k_energy_barrier(int type, int n,
             X0[k] = type >= T_EEM ? ld3(x0, id[k]) : mk(0, 0, 0);
         }
         double e;
-        barrier_row(type, X, X0, dh2, kappa, 0, &e, nullptr, nullptr);
+        barrier_row(type, X, X0, dh2, kap, 0, &e, nullptr, nullptr);
         acc += e;
     }
     const double s = block_sum(acc, sh);
@@ -247,10 +251,10 @@ int launch_elasticity(int nT, const int* tets, const double* x, const double* dm
     return FIPC_OK;
 }
 
-int launch_barrier_rows(int type, int n, const int* rows, const double* x, const double* x0, double dh2, double kappa, double* E,
-                        double* g, double* Hb, int* status, cudaStream_t s) {
+int launch_barrier_rows(int type, int n, const int* rows, const double* x, const double* x0, double dh2, double kappa,
+                        const double* kap_s, const int* vscene, double* E, double* g, double* Hb, int* status, cudaStream_t s) {
     if (n <= 0) return FIPC_OK;
-    k_barrier_rows<<<nblk(n, 128), 128, 0, s>>>(type, n, (const int4*)rows, x, x0, dh2, kappa, E, g, Hb, status);
+    k_barrier_rows<<<nblk(n, 128), 128, 0, s>>>(type, n, (const int4*)rows, x, x0, dh2, kappa, kap_s, vscene, E, g, Hb, status);
     FIPC_LAUNCHED();
     FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
@@ -268,6 +272,7 @@ int launch_energy(const fipc_ctx* c, const double* x, const double* xt, const in
     for (int t = 0; t < N_TYPES; ++t) {
         if (counts[t] <= 0) continue;
         k_energy_barrier<<<RED_BLOCKS, RED_THREADS, 0, s>>>(t, counts[t], (const int4*)rows[t], x, c->x0, c->dhat2, c->kappa,
+                                                           c->n_scenes > 1 ? c->s_kappa : nullptr, c->v_scene,
                                                            part + (size_t)np * RED_BLOCKS);
         FIPC_LAUNCHED();
         ++np;
@@ -303,7 +308,7 @@ int fipc_barrier_rows(int type, int n_rows, const int* rows, const double* x, co
                       double* E, double* g, double* H, void* stream) {
     if (type < 0 || type >= N_TYPES || n_rows < 0 || !rows || !x || (type >= T_EEM && !x0)) return FIPC_ERR_ARGUMENT;
     if ((g == nullptr) != (H == nullptr)) return FIPC_ERR_ARGUMENT;
-    return launch_barrier_rows(type, n_rows, rows, x, x0, dhat2, kappa, E, g, H, nullptr, (cudaStream_t)stream);
+    return launch_barrier_rows(type, n_rows, rows, x, x0, dhat2, kappa, nullptr, nullptr, E, g, H, nullptr, (cudaStream_t)stream);
 }
 
 int fipc_ccd_pairs(int kind, int n, const double* xq, const double* pq, double eta, double* toc, void* stream) {

@@ -1,0 +1,117 @@
+// Shared by the single-scene and batched PCG: the system operands and the per-row product
+// w_i = sum_j A_ij v_j over the elastic sliced-ELL rows and the contact block-CSR rows.
+#pragma once
+
+#include "ctx.cuh"
+
+namespace fipc {
+
+struct PCGArgs {
+    int nV;
+    const int *soff, *scol, *rlen;   // elastic matrix, sliced-ELL
+    const double* sval;
+    const int *crp, *cci;            // contact matrix, block-CSR
+    const double* cva;
+    const unsigned char* fixed;
+    const int* diag_spos;
+    double *x, *r, *u, *w, *p, *s, *minv;   // u: stride 4 (padded); the others stride 3
+    double* part;                    // [3][nblk]
+    double* sc;                      // scalars, see SC_*
+    int* flag;                       // [0] done, [1] iterations, [2] ticket
+};
+enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
+constexpr int PCG_THREADS = 128;
+
+// w_i = sum_j A_ij v_j over the elastic (sliced-ELL) and contact (block-CSR) rows of vertex i;
+// v is stored with stride ST doubles per vertex (ST = 4: 32-byte aligned, two vector loads)
+template <int ST>
+__device__ __forceinline__ void load_v(const double* __restrict__ v, int j, double& a, double& b, double& c) {
+    if (ST == 4) {
+        const double2 ab = __ldg(reinterpret_cast<const double2*>(v + 4 * (size_t)j));
+        a = ab.x;
+        b = ab.y;
+        c = __ldg(v + 4 * (size_t)j + 2);
+    } else {
+        a = __ldg(v + 3 * (size_t)j);
+        b = __ldg(v + 3 * (size_t)j + 1);
+        c = __ldg(v + 3 * (size_t)j + 2);
+    }
+}
+
+template <int ST>
+__device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double* __restrict__ v, double& y0, double& y1, double& y2) {
+    y0 = y1 = y2 = 0.0;
+    const int sl = i >> 5, lane = i & 31;
+    const int base = a.soff[sl], len = a.rlen[i];
+    int k = 0;
+    // two blocks per trip: their index, value and vector loads are independent
+    for (; k + 1 < len; k += 2) {
+        const size_t s0 = (size_t)(base + k), s1 = s0 + 1;
+        const int j0 = __ldg(a.scol + s0 * 32 + lane), j1 = __ldg(a.scol + s1 * 32 + lane);
+        const double* B = a.sval + s0 * 288 + lane;
+        const double* C = a.sval + s1 * 288 + lane;
+        double b[9], c[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            b[q] = __ldg(B + 32 * q);
+            c[q] = __ldg(C + 32 * q);
+        }
+        double p0, p1, p2, q0, q1, q2;
+        load_v<ST>(v, j0, p0, p1, p2);
+        load_v<ST>(v, j1, q0, q1, q2);
+        // pure FMA chains: three DFMA per block row
+        y0 = fma(b[0], p0, fma(b[1], p1, fma(b[2], p2, y0)));
+        y1 = fma(b[3], p0, fma(b[4], p1, fma(b[5], p2, y1)));
+        y2 = fma(b[6], p0, fma(b[7], p1, fma(b[8], p2, y2)));
+        y0 = fma(c[0], q0, fma(c[1], q1, fma(c[2], q2, y0)));
+        y1 = fma(c[3], q0, fma(c[4], q1, fma(c[5], q2, y1)));
+        y2 = fma(c[6], q0, fma(c[7], q1, fma(c[8], q2, y2)));
+    }
+    if (k < len) {
+        const size_t s0 = (size_t)(base + k);
+        const int j0 = __ldg(a.scol + s0 * 32 + lane);
+        const double* B = a.sval + s0 * 288 + lane;
+        double p0, p1, p2;
+        load_v<ST>(v, j0, p0, p1, p2);
+        y0 = fma(__ldg(B + 0), p0, fma(__ldg(B + 32), p1, fma(__ldg(B + 64), p2, y0)));
+        y1 = fma(__ldg(B + 96), p0, fma(__ldg(B + 128), p1, fma(__ldg(B + 160), p2, y1)));
+        y2 = fma(__ldg(B + 192), p0, fma(__ldg(B + 224), p1, fma(__ldg(B + 256), p2, y2)));
+    }
+    for (int e = a.crp[i]; e < a.crp[i + 1]; ++e) {
+        const int j = a.cci[e];
+        const double* B = a.cva + 9 * (size_t)e;
+        double v0, v1, v2;
+        load_v<ST>(v, j, v0, v1, v2);
+        y0 = fma(B[0], v0, fma(B[1], v1, fma(B[2], v2, y0)));
+        y1 = fma(B[3], v0, fma(B[4], v1, fma(B[5], v2, y1)));
+        y2 = fma(B[6], v0, fma(B[7], v1, fma(B[8], v2, y2)));
+    }
+}
+
+// block-Jacobi preconditioner: the inverse of vertex i's 3x3 diagonal block (elastic + contact);
+// identity at Dirichlet vertices
+__device__ __forceinline__ void jacobi_block_inverse(const PCGArgs& a, int i, bool fx, double (&Mi)[9]) {
+    if (fx) {
+        for (int k = 0; k < 9; ++k) Mi[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    } else {
+        double D[9];
+        const double* E = a.sval + (size_t)(a.diag_spos[i] >> 5) * 288 + (a.diag_spos[i] & 31);
+        for (int k = 0; k < 9; ++k) D[k] = E[32 * k];
+        for (int k = a.crp[i]; k < a.crp[i + 1]; ++k)
+            if (a.cci[k] == i)
+                for (int q = 0; q < 9; ++q) D[q] += a.cva[9 * (size_t)k + q];
+        const double c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8], c02 = D[3] * D[7] - D[4] * D[6];
+        const double id = 1.0 / (D[0] * c00 + D[1] * c01 + D[2] * c02);
+        Mi[0] = c00 * id;
+        Mi[1] = (D[2] * D[7] - D[1] * D[8]) * id;
+        Mi[2] = (D[1] * D[5] - D[2] * D[4]) * id;
+        Mi[3] = c01 * id;
+        Mi[4] = (D[0] * D[8] - D[2] * D[6]) * id;
+        Mi[5] = (D[2] * D[3] - D[0] * D[5]) * id;
+        Mi[6] = c02 * id;
+        Mi[7] = (D[1] * D[6] - D[0] * D[7]) * id;
+        Mi[8] = (D[0] * D[4] - D[1] * D[3]) * id;
+    }
+}
+
+}  // namespace fipc

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include "ctx.cuh"
+#include "pcg.cuh"
 #include "profile.cuh"
 
 namespace fipc {
@@ -175,84 +176,6 @@ __global__ void k_contact_rowptr(int nV, int nu, const unsigned long long* __res
 //   p = u + beta p, s = w + beta s, x += alpha p, r -= alpha s, u = M^-1 r.
 // Dot products: per-block partials; the last block to finish (atomic ticket) sums them in block
 // order and derives alpha/beta, so the scalars are bitwise reproducible and need no launch.
-struct PCGArgs {
-    int nV;
-    const int *soff, *scol, *rlen;   // elastic matrix, sliced-ELL
-    const double* sval;
-    const int *crp, *cci;            // contact matrix, block-CSR
-    const double* cva;
-    const unsigned char* fixed;
-    const int* diag_spos;
-    double *x, *r, *u, *w, *p, *s, *minv;   // u: stride 4 (padded); the others stride 3
-    double* part;                    // [3][nblk]
-    double* sc;                      // scalars, see SC_*
-    int* flag;                       // [0] done, [1] iterations, [2] ticket
-};
-enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
-constexpr int PCG_THREADS = 128;
-
-// w_i = sum_j A_ij v_j over the elastic (sliced-ELL) and contact (block-CSR) rows of vertex i;
-// v is stored with stride ST doubles per vertex (ST = 4: 32-byte aligned, two vector loads)
-template <int ST>
-__device__ __forceinline__ void load_v(const double* __restrict__ v, int j, double& a, double& b, double& c) {
-    if (ST == 4) {
-        const double2 ab = __ldg(reinterpret_cast<const double2*>(v + 4 * (size_t)j));
-        a = ab.x;
-        b = ab.y;
-        c = __ldg(v + 4 * (size_t)j + 2);
-    } else {
-        a = __ldg(v + 3 * (size_t)j);
-        b = __ldg(v + 3 * (size_t)j + 1);
-        c = __ldg(v + 3 * (size_t)j + 2);
-    }
-}
-
-template <int ST>
-__device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double* __restrict__ v, double& y0, double& y1, double& y2) {
-    y0 = y1 = y2 = 0.0;
-    const int sl = i >> 5, lane = i & 31;
-    const int base = a.soff[sl], len = a.rlen[i];
-    int k = 0;
-    // two blocks per trip: their index, value and vector loads are independent
-    for (; k + 1 < len; k += 2) {
-        const size_t s0 = (size_t)(base + k), s1 = s0 + 1;
-        const int j0 = __ldg(a.scol + s0 * 32 + lane), j1 = __ldg(a.scol + s1 * 32 + lane);
-        const double* B = a.sval + s0 * 288 + lane;
-        const double* C = a.sval + s1 * 288 + lane;
-        double b[9], c[9];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            b[q] = __ldg(B + 32 * q);
-            c[q] = __ldg(C + 32 * q);
-        }
-        double p0, p1, p2, q0, q1, q2;
-        load_v<ST>(v, j0, p0, p1, p2);
-        load_v<ST>(v, j1, q0, q1, q2);
-        y0 += b[0] * p0 + b[1] * p1 + b[2] * p2 + c[0] * q0 + c[1] * q1 + c[2] * q2;
-        y1 += b[3] * p0 + b[4] * p1 + b[5] * p2 + c[3] * q0 + c[4] * q1 + c[5] * q2;
-        y2 += b[6] * p0 + b[7] * p1 + b[8] * p2 + c[6] * q0 + c[7] * q1 + c[8] * q2;
-    }
-    if (k < len) {
-        const size_t s0 = (size_t)(base + k);
-        const int j0 = __ldg(a.scol + s0 * 32 + lane);
-        const double* B = a.sval + s0 * 288 + lane;
-        double p0, p1, p2;
-        load_v<ST>(v, j0, p0, p1, p2);
-        y0 += __ldg(B + 0) * p0 + __ldg(B + 32) * p1 + __ldg(B + 64) * p2;
-        y1 += __ldg(B + 96) * p0 + __ldg(B + 128) * p1 + __ldg(B + 160) * p2;
-        y2 += __ldg(B + 192) * p0 + __ldg(B + 224) * p1 + __ldg(B + 256) * p2;
-    }
-    for (int e = a.crp[i]; e < a.crp[i + 1]; ++e) {
-        const int j = a.cci[e];
-        const double* B = a.cva + 9 * (size_t)e;
-        double v0, v1, v2;
-        load_v<ST>(v, j, v0, v1, v2);
-        y0 += B[0] * v0 + B[1] * v1 + B[2] * v2;
-        y1 += B[3] * v0 + B[4] * v1 + B[5] * v2;
-        y2 += B[6] * v0 + B[7] * v1 + B[8] * v2;
-    }
-}
-
 // block sums of up to 3 values into part[c * nblk + block]; returns true in every thread of
 // the last block to finish, which then reduces the partials with final_sums
 template <int NV>
@@ -310,31 +233,11 @@ __device__ __forceinline__ void final_sums(const PCGArgs& a, double (&out)[NV]) 
 // residual of the initial guess, block-Jacobi inverse, u = M^-1 r; partials of (r,r)
 __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const double* __restrict__ rhs, double rtol) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double rr = 0.0;
+    double rr = 0.0, bb = 0.0;
     if (i < a.nV) {
         double Mi[9];
         const bool fx = a.fixed[i] != 0;
-        if (fx) {
-            for (int k = 0; k < 9; ++k) Mi[k] = (k % 4 == 0) ? 1.0 : 0.0;
-        } else {
-            double D[9];
-            const double* E = a.sval + (size_t)(a.diag_spos[i] >> 5) * 288 + (a.diag_spos[i] & 31);
-            for (int k = 0; k < 9; ++k) D[k] = E[32 * k];
-            for (int k = a.crp[i]; k < a.crp[i + 1]; ++k)
-                if (a.cci[k] == i)
-                    for (int q = 0; q < 9; ++q) D[q] += a.cva[9 * (size_t)k + q];
-            const double c00 = D[4] * D[8] - D[5] * D[7], c01 = D[5] * D[6] - D[3] * D[8], c02 = D[3] * D[7] - D[4] * D[6];
-            const double id = 1.0 / (D[0] * c00 + D[1] * c01 + D[2] * c02);
-            Mi[0] = c00 * id;
-            Mi[1] = (D[2] * D[7] - D[1] * D[8]) * id;
-            Mi[2] = (D[1] * D[5] - D[2] * D[4]) * id;
-            Mi[3] = c01 * id;
-            Mi[4] = (D[0] * D[8] - D[2] * D[6]) * id;
-            Mi[5] = (D[2] * D[3] - D[0] * D[5]) * id;
-            Mi[6] = c02 * id;
-            Mi[7] = (D[1] * D[6] - D[0] * D[7]) * id;
-            Mi[8] = (D[0] * D[4] - D[1] * D[3]) * id;
-        }
+        jacobi_block_inverse(a, i, fx, Mi);
         for (int k = 0; k < 9; ++k) a.minv[9 * (size_t)i + k] = Mi[k];
         double y0, y1, y2;
         row_apply<3>(a, i, a.x, y0, y1, y2);
@@ -342,6 +245,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const doub
         a.r[3 * i] = r0;
         a.r[3 * i + 1] = r1;
         a.r[3 * i + 2] = r2;
+        if (!fx) bb = rhs[3 * i] * rhs[3 * i] + rhs[3 * i + 1] * rhs[3 * i + 1] + rhs[3 * i + 2] * rhs[3 * i + 2];
         for (int d = 0; d < 3; ++d) {
             a.u[4 * i + d] = Mi[3 * d] * r0 + Mi[3 * d + 1] * r1 + Mi[3 * d + 2] * r2;
             a.p[3 * i + d] = 0.0;
@@ -350,17 +254,18 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const doub
         a.u[4 * i + 3] = 0.0;
         rr = r0 * r0 + r1 * r1 + r2 * r2;
     }
-    const double v[1] = {rr};
-    if (block_partials<1>(a, v)) {
-        double tt[1];
-        final_sums<1>(a, tt);
+    // the tolerance is relative to |b| on the free DOFs (= |r0| when starting from zero)
+    const double v[2] = {rr, bb};
+    if (block_partials<2>(a, v)) {
+        double tt[2];
+        final_sums<2>(a, tt);
         if (threadIdx.x != 0) return;
         const double t = tt[0];
         a.sc[SC_RR0] = t;
-        a.sc[SC_TOL2] = rtol * rtol * t;
+        a.sc[SC_TOL2] = rtol * rtol * tt[1];
         a.sc[SC_GAMMA] = 1.0;
         a.sc[SC_ALPHA] = 1.0;
-        a.flag[0] = t == 0.0 ? 1 : 0;
+        a.flag[0] = (t == 0.0 || t <= rtol * rtol * tt[1]) ? 1 : 0;
         a.flag[1] = 0;
         a.flag[2] = 0;
     }
@@ -443,8 +348,8 @@ static int cub_call(fipc_ctx* c, F&& f) {
 
 int launch_elasticity(int nT, const int* tets, const double* x, const double* dminv, const double* vol, const double* lam,
                       const double* mu, double dt, double* E, double* g, double* Hu, cudaStream_t s);
-int launch_barrier_rows(int type, int n, const int* rows, const double* x, const double* x0, double dh2, double kappa, double* E,
-                        double* g, double* Hb, int* status, cudaStream_t s);
+int launch_barrier_rows(int type, int n, const int* rows, const double* x, const double* x0, double dh2, double kappa,
+                        const double* kap_s, const int* vscene, double* E, double* g, double* Hb, int* status, cudaStream_t s);
 
 // compute_hessian_and_gradient (NEWTON_IPC.py:736-747) for the current constraint lists
 int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t s) {
@@ -484,7 +389,8 @@ int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t
         tt.ent0[t] = eoff;
         if (c->h_counts[t]) {
             FIPC_CUDA(cudaMemcpyAsync(all + off, c->rows[t].p, 16ll * c->h_counts[t], cudaMemcpyDeviceToDevice, s));
-            st = launch_barrier_rows(t, c->h_counts[t], c->rows[t].as<int>(), x, c->x0, c->dhat2, c->kappa, nullptr,
+            st = launch_barrier_rows(t, c->h_counts[t], c->rows[t].as<int>(), x, c->x0, c->dhat2, c->kappa,
+                                     c->n_scenes > 1 ? c->s_kappa : nullptr, c->v_scene, nullptr,
                                      c->c_g.as<double>() + 12ll * off, c->c_H.as<double>() + 144ll * off, nullptr, s);
             if (st) return st;
         }

@@ -1,0 +1,426 @@
+"""Learned Newton warm start: a per-vertex MLP corrects the inertial guess of each time step.
+
+The network (55 inputs -> 128 -> 128 -> 128 -> 3, GELU, FP32) runs and trains on the
+hand-written CUDA kernels of libfastipc.so: features, forward, backward, MSE and Adam.  Torch
+only holds the buffers.
+
+Guess used by ``NewtonIPC.step`` after ``move_nodes`` (the reference starts Newton at x^n):
+1. The inertial predictor d0 = xTilde - x^n on free vertices (x^n + dt v + dt^2 g).
+2. The learned displacement d = d0 + s h out, with out the network's output, h the hash cell
+   (mean boundary edge length) and s the target scale fixed at training time.
+3. Each candidate step is filtered like a Newton direction.  alpha comes from the CCD and
+   inversion filter, and is halved while any edge crosses a triangle.
+4. Start from whichever of x^n, the filtered inertial step and the filtered learned step has the
+   lowest incremental potential.  The learned guess falls back to the inertial one, and that
+   one to the reference's x^n.
+5. Newton then runs to the reference's unchanged tolerance.  A guess never admits intersection
+   and never raises the starting energy.
+
+Training data are transitions (x^n, v^n) -> x^{n+1} generated by the plain solver.  The
+target per free vertex is (x^{n+1} - xTilde) / (s h): the part of the step that inertia does
+not predict.  The last layer starts at zero, so an untrained network gives the inertial guess.
+"""
+import ctypes
+import json
+import time
+
+import numpy as np
+import torch
+
+from . import _native as N
+from ._native import check
+
+F32 = torch.float32
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+class WarmStartMLP:
+    IN, H, OUT = 64, 128, 4
+
+    def __init__(self, device='cuda:0', seed=0, params=None, scale=1.0):
+        self.scale = float(scale)
+        self.device = torch.device(device)
+        self.nparam = int(N.lib().fipc_mlp_param_count())
+        if params is None:
+            from_np = _init_params(seed)
+            params = torch.tensor(from_np, dtype=F32)
+        self.params = params.to(self.device, F32).contiguous()
+        assert self.params.numel() == self.nparam
+        self.grads = torch.zeros_like(self.params)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.t = 0
+        self._scratch_n = 0
+
+    def _scratch(self, n):
+        if n > self._scratch_n:
+            dev = self.device
+            self.Z = torch.empty(3 * n * self.H, dtype=F32, device=dev)
+            self.A = torch.empty(3 * n * self.H, dtype=F32, device=dev)
+            self.dA = torch.empty(2 * n * self.H, dtype=F32, device=dev)
+            self.out = torch.empty((n, self.OUT), dtype=F32, device=dev)
+            self.dout = torch.empty((n, self.OUT), dtype=F32, device=dev)
+            self.part = torch.empty((n + 255) // 256 + 1, dtype=F32, device=dev)
+            self.loss = torch.empty(1, dtype=F32, device=dev)
+            self._scratch_n = n
+
+    def forward(self, X):
+        n = X.shape[0]
+        self._scratch(n)
+        check(N.lib().fipc_mlp_forward(n, _p(X), _p(self.params), _p(self.Z), _p(self.A), _p(self.out), N.stream()), 'mlp_forward')
+        return self.out[:n]
+
+    def train_step(self, X, Y, lr=1e-3):
+        """One Adam step on the mean squared error of batch (X [n,64], Y [n,4]); returns the loss."""
+        n = X.shape[0]
+        self.forward(X)
+        L = N.lib()
+        check(L.fipc_mlp_mse(n, _p(self.out), _p(Y), _p(self.dout), _p(self.part), _p(self.loss), N.stream()), 'mlp_mse')
+        check(L.fipc_mlp_backward(n, _p(X), _p(self.params), _p(self.Z), _p(self.A), _p(self.dout), _p(self.grads), _p(self.dA),
+                                  N.stream()), 'mlp_backward')
+        self.t += 1
+        check(L.fipc_mlp_adam(self.nparam, _p(self.params), _p(self.grads), _p(self.m), _p(self.v), ctypes.c_float(lr),
+                              ctypes.c_float(0.9), ctypes.c_float(0.999), ctypes.c_float(1e-8), self.t, N.stream()), 'mlp_adam')
+        return self.loss
+
+    def save(self, path):
+        np.savez(path, params=self.params.cpu().numpy(), scale=np.float64(self.scale))
+
+    @classmethod
+    def load(cls, path, device='cuda:0'):
+        d = np.load(path)
+        return cls(device=device, params=torch.from_numpy(d['params']), scale=float(d['scale']))
+
+
+def _init_params(seed):
+    rng = np.random.default_rng(seed)
+    parts = []
+    for name, shp in [('W1', (128, 64)), ('b1', (128,)), ('W2', (128, 128)), ('b2', (128,)), ('W3', (128, 128)), ('b3', (128,)),
+                      ('W4', (4, 128)), ('b4', (4,))]:
+        if name.startswith('W'):
+            w = rng.normal(size=shp) * np.sqrt(2.0 / shp[1])
+            parts.append(w * 0.0 if name == 'W4' else w)
+        else:
+            parts.append(np.zeros(shp))
+    return np.concatenate([a.ravel() for a in parts]).astype(np.float32)
+
+
+def features(sim, X=None):
+    """Per-vertex inputs at the current state (constraint lists of the last find_constraints)."""
+    if X is None:
+        X = torch.empty((sim.nV, WarmStartMLP.IN), dtype=F32, device=sim.device)
+    h = 1.0 / sim.inv_dx
+    check(N.lib().fipc_mlp_features(sim.ctx, N.dptr(sim.x, torch.float64), N.dptr(sim.v, torch.float64),
+                                    N.dptr(sim.dx_prev, torch.float64), ctypes.c_double(h), _p(X), N.stream()), 'mlp_features')
+    return X
+
+
+class LearnedStart:
+    """``NewtonIPC.initial_guess`` hook: the lowest-energy filtered start among x^n, the inertial
+    step and (kind 'mlp') the learned step.
+
+    ``chosen`` counts which candidate each step started from; ``alphas`` the filtered step
+    lengths of the chosen candidates.
+    """
+
+    def __init__(self, model=None, kind='mlp'):
+        assert kind in ('mlp', 'inertial')
+        assert kind == 'inertial' or model is not None
+        self.model, self.kind = model, kind
+        self.chosen = {'plain': 0, 'inertial': 0, 'mlp': 0}
+        self.alphas = []
+        self._X = None
+
+    @property
+    def accepted(self):
+        return self.chosen['inertial'] + self.chosen['mlp']
+
+    @property
+    def fallback(self):
+        return self.chosen['plain']
+
+    def inertial(self, sim):
+        free = (sim.fixed == 0).unsqueeze(1)
+        return torch.where(free, sim.xTilde - sim.x, torch.zeros_like(sim.x))
+
+    def learned(self, sim, d0):
+        """d0 + s h out; needs the constraint lists of the current positions (features)."""
+        if self._X is None or self._X.shape[0] != sim.nV:
+            self._X = torch.empty((sim.nV, WarmStartMLP.IN), dtype=F32, device=sim.device)
+        X = features(sim, self._X)
+        out = self.model.forward(X)
+        d = d0 + out[:, :3].to(torch.float64) * (self.model.scale / sim.inv_dx)
+        return torch.where((sim.fixed == 0).unsqueeze(1), d, torch.zeros_like(d))
+
+    def _filtered(self, sim, d):
+        """x = x^n + alpha d with alpha from the CCD filter and collision halving; its energy."""
+        sim.data_sol.copy_(d)
+        alpha = sim.compute_intersection_free_step_size()
+        sim.apply_sol(alpha)
+        k = 0
+        while sim.check_collision():
+            alpha /= 2.0
+            sim.apply_sol(alpha)
+            k += 1
+            if k > sim.max_halvings:
+                return None, None
+        sim.find_constraints()
+        return alpha, sim.compute_energy()
+
+    def __call__(self, sim, f):
+        sim.find_constraints()
+        e_best, name_best, d_best, a_best = sim.compute_energy(), 'plain', None, 0.0
+        sim.save_xPrev()
+        d0 = self.inertial(sim)
+        cands = [('inertial', d0)]
+        if self.kind == 'mlp':
+            cands.append(('mlp', self.learned(sim, d0)))   # features at x^n (lists found above)
+        for name, d in cands:
+            alpha, e = self._filtered(sim, d)
+            if alpha is not None and e < e_best:
+                e_best, name_best, d_best, a_best = e, name, d, alpha
+        if d_best is None:
+            sim.x.copy_(sim.xPrev)
+        else:
+            sim.data_sol.copy_(d_best)
+            sim.apply_sol(a_best)
+            self.alphas.append(a_best)
+        self.chosen[name_best] += 1
+
+
+# ---------------------------------------------------------------------- data and training
+class _Recorder:
+    """Hook that records (features, free mask, inertial predictor) at each step's start."""
+
+    def __init__(self, inner=None):
+        self.pending = None
+        self.inner = inner
+
+    def __call__(self, sim, f):
+        sim.find_constraints()
+        self.pending = (features(sim).clone(), (sim.fixed == 0).clone(), sim.xTilde.clone())
+        if self.inner is not None:
+            self.inner(sim, f)
+
+
+def collect(scene, steps, device='cuda:0', pcg_rtol=1e-6, start=0):
+    """Run the solver (inertial start, which converges to the same steps as the plain one) for
+    ``steps`` steps; returns (X [n,64], Y [n,4]) over the free vertices of steps >= start,
+    Y = (x^{n+1} - xTilde) / h."""
+    from .newton import NewtonIPC
+    sim = NewtonIPC(scene, device=device, pcg_rtol=pcg_rtol)
+    rec = _Recorder(LearnedStart(kind='inertial'))
+    sim.initial_guess = rec
+    h = 1.0 / sim.inv_dx
+    Xs, Ys = [], []
+    for f in range(steps):
+        sim.step(f)
+        if f < start:
+            continue
+        X, free, xt = rec.pending
+        Y = torch.zeros((sim.nV, 4), dtype=F32, device=sim.device)
+        Y[:, :3] = ((sim.x - xt) / h).to(F32)
+        Xs.append(X[free])
+        Ys.append(Y[free])
+    sim.close()
+    return torch.cat(Xs), torch.cat(Ys)
+
+
+def train(model, X, Y, epochs=30, batch=8192, lr=1e-3, seed=0, log=None):
+    """Mini-batch Adam on the CUDA kernels with a cosine learning-rate decay."""
+    g = torch.Generator(device='cpu').manual_seed(seed)
+    n = X.shape[0]
+    nb = max(1, n // batch)
+    total = epochs * nb
+    step = 0
+    hist = []
+    for ep in range(epochs):
+        perm = torch.randperm(n, generator=g).to(X.device)
+        acc = torch.zeros((), device=X.device)
+        for b in range(nb):
+            idx = perm[b * batch:(b + 1) * batch]
+            cur = lr * 0.5 * (1 + np.cos(np.pi * step / total))
+            acc += model.train_step(X[idx].contiguous(), Y[idx].contiguous(), lr=cur)[0]
+            step += 1
+        hist.append(float(acc) / nb)
+        if log:
+            log(f'epoch {ep} loss {hist[-1]:.4e}')
+    return hist
+
+
+def evaluate(model, X, Y):
+    out = model.forward(X)
+    return float(((out[:, :3] - Y[:, :3]) ** 2).mean())
+
+
+def _result(sim, guess, steps, wall, intersect):
+    out = {'steps': steps, 'newton': int(sum(sim.newton_iters)), 'pcg': int(sum(sim.pcg_iters)), 'wall_s': wall,
+           'intersecting_steps': intersect, 'newton_per_step': list(map(int, sim.newton_iters))}
+    if guess is not None:
+        out['chosen'] = dict(guess.chosen)
+    return out
+
+
+def run_scene(scene, steps, guess=None, device='cuda:0', pcg_rtol=1e-6):
+    """Plain (guess None) or guessed run; returns counters and the final positions."""
+    from .newton import NewtonIPC
+    sim = NewtonIPC(scene, device=device, pcg_rtol=pcg_rtol)
+    sim.initial_guess = guess
+    intersect = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for f in range(steps):
+        sim.step(f)
+        intersect += int(sim.check_collision())
+    torch.cuda.synchronize()
+    out = _result(sim, guess, steps, time.perf_counter() - t0, intersect)
+    x = sim.x.cpu().numpy()
+    sim.close()
+    return out, x
+
+
+def _split(X, Y, seed=0):
+    g = torch.Generator(device='cpu').manual_seed(seed)
+    perm = torch.randperm(X.shape[0], generator=g).to(X.device)
+    nval = X.shape[0] // 10
+    return X[perm[nval:]].contiguous(), Y[perm[nval:]].contiguous(), X[perm[:nval]].contiguous(), Y[perm[:nval]].contiguous()
+
+
+def fit(X, Y, device='cuda:0', epochs=30, log=print, seed=0):
+    """Train a model on (X, Y in h units); the target scale is the RMS of Y.  Returns the model
+    and its statistics (validation MSE of the network and of the inertial guess, in h^2)."""
+    Xt, Yt, Xv, Yv = _split(X, Y, seed)
+    scale = float(Yt[:, :3].pow(2).mean().sqrt())
+    model = WarmStartMLP(device, seed=seed, scale=scale)
+    t1 = time.perf_counter()
+    hist = train(model, Xt, Yt / scale, epochs=epochs, log=log)
+    torch.cuda.synchronize()
+    stats = {'rows_train': int(Xt.shape[0]), 'rows_val': int(Xv.shape[0]), 'train_s': time.perf_counter() - t1, 'scale_h': scale,
+             'loss_hist': hist, 'val_mse_h2': evaluate(model, Xv, Yv / scale) * scale ** 2,
+             'val_mse_h2_inertial': float(Yv[:, :3].pow(2).mean())}
+    return model, stats
+
+
+def _small_train_scenes():
+    from . import scenes as S
+    out = [(S.twisted_bar(nx=100, ny=6, nz=6, seed=s, speed=sp), 60) for s, sp in [(0, np.pi), (1, 0.5 * np.pi), (2, 1.5 * np.pi)]]
+    out += [(S.two_cubes(n=6, seed=s), 40) for s in range(4)]
+    out += [(S.cube_lattice(m=2, n=4, seed=s), 40) for s in range(6)]
+    return out
+
+
+def _small_test_scenes():
+    from . import scenes as S
+    return [('twisted_bar_200x10x10', S.twisted_bar(nx=200, ny=10, nz=10, seed=7), 40),
+            ('two_cubes_n8', S.two_cubes(n=8, seed=11), 40),
+            ('cube_lattice_8_seed20', S.cube_lattice(m=2, n=4, seed=20), 40),
+            ('cube_lattice_8_seed21', S.cube_lattice(m=2, n=4, seed=21), 40)]
+
+
+def experiment_small(out_dir, device='cuda:0', epochs=30, log=print):
+    """Train on small seed-varied scenes, compare plain / inertial / MLP starts on unseen ones."""
+    import os
+    os.makedirs(out_dir, exist_ok=True)
+    t0 = time.perf_counter()
+    Xs, Ys = [], []
+    for sc, steps in _small_train_scenes():
+        X, Y = collect(sc, steps, device)
+        Xs.append(X)
+        Ys.append(Y)
+        log(f'collected {sc.name} {sc.meta}: {X.shape[0]} rows')
+    res = {'collect_s': time.perf_counter() - t0}
+    model, stats = fit(torch.cat(Xs), torch.cat(Ys), device, epochs, log)
+    res.update(stats)
+    model.save(os.path.join(out_dir, 'warmstart_small.npz'))
+    res['scenes'] = {}
+    for name, sc, steps in _small_test_scenes():
+        r = {}
+        xs = {}
+        for mode in ('plain', 'inertial', 'mlp'):
+            guess = None if mode == 'plain' else LearnedStart(model if mode == 'mlp' else None, kind=mode)
+            r[mode], xs[mode] = run_scene(sc, steps, guess, device)
+        for mode in ('inertial', 'mlp'):
+            r[mode]['max_dev_vs_plain'] = float(np.abs(xs[mode] - xs['plain']).max())
+        res['scenes'][name] = r
+        log(f"{name}: newton plain {r['plain']['newton']} inertial {r['inertial']['newton']} mlp {r['mlp']['newton']}; "
+            f"wall {r['plain']['wall_s']:.2f} / {r['inertial']['wall_s']:.2f} / {r['mlp']['wall_s']:.2f} s")
+    with open(os.path.join(out_dir, 'warmstart_small.json'), 'w') as fh:
+        json.dump(res, fh, indent=1)
+    return res
+
+
+def experiment_bar(out_dir, nx=400, train_steps=30, eval_steps=30, device='cuda:0', epochs=20, log=print, pcg_rtol=1e-6):
+    """The twisted bar with its own transitions: collect steps [0, train_steps) with the
+    inertial start, train, then run steps [train_steps, train_steps + eval_steps) from the same
+    state with the plain, inertial and learned starts."""
+    import os
+    from . import scenes as S
+    from .newton import NewtonIPC
+    os.makedirs(out_dir, exist_ok=True)
+    sc = S.twisted_bar(nx=nx, ny=20, nz=20, size=(nx / 400.0, 0.05, 0.05), seed=0)
+    sim = NewtonIPC(sc, device=device, pcg_rtol=pcg_rtol)
+    rec = _Recorder(LearnedStart(kind='inertial'))
+    sim.initial_guess = rec
+    h = 1.0 / sim.inv_dx
+    Xs, Ys = [], []
+    t0 = time.perf_counter()
+    for f in range(train_steps):
+        sim.step(f)
+        X, free, xt = rec.pending
+        Y = torch.zeros((sim.nV, 4), dtype=F32, device=sim.device)
+        Y[:, :3] = ((sim.x - xt) / h).to(F32)
+        Xs.append(X[free])
+        Ys.append(Y[free])
+    res = {'scene': sc.meta, 'train_steps': train_steps, 'eval_steps': eval_steps, 'collect_s': time.perf_counter() - t0}
+    model, stats = fit(torch.cat(Xs), torch.cat(Ys), device, epochs, log)
+    del Xs, Ys
+    res.update(stats)
+    model.save(os.path.join(out_dir, f'warmstart_bar{nx}.npz'))
+    snap = (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone())
+    xs = {}
+    for mode in ('plain', 'inertial', 'mlp'):
+        sim.x.copy_(snap[0])
+        sim.v.copy_(snap[1])
+        sim.dx_prev.copy_(snap[2])
+        sim.newton_iters, sim.pcg_iters = [], []
+        guess = None if mode == 'plain' else LearnedStart(model if mode == 'mlp' else None, kind=mode)
+        sim.initial_guess = guess
+        inter = 0
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        for f in range(train_steps, train_steps + eval_steps):
+            sim.step(f)
+            inter += int(sim.check_collision())
+        torch.cuda.synchronize()
+        res[mode] = _result(sim, guess, eval_steps, time.perf_counter() - t1, inter)
+        xs[mode] = sim.x.cpu().numpy()
+        log(f"bar {mode}: newton {res[mode]['newton']} pcg {res[mode]['pcg']} wall {res[mode]['wall_s']:.2f} s")
+    for mode in ('inertial', 'mlp'):
+        res[mode]['max_dev_vs_plain'] = float(np.abs(xs[mode] - xs['plain']).max())
+    sim.close()
+    with open(os.path.join(out_dir, f'warmstart_bar{nx}.json'), 'w') as fh:
+        json.dump(res, fh, indent=1)
+    return res
+
+
+def main(argv=None):
+    import argparse
+    ap = argparse.ArgumentParser(description='train and evaluate the learned Newton warm start')
+    ap.add_argument('--out', default='warmstart_out')
+    ap.add_argument('--epochs', type=int, default=30)
+    ap.add_argument('--small', action='store_true', help='seed-varied small scenes')
+    ap.add_argument('--bar', type=int, default=0, help='twisted bar with nx hexes along its axis (0: skip)')
+    ap.add_argument('--train-steps', type=int, default=30)
+    ap.add_argument('--eval-steps', type=int, default=30)
+    a = ap.parse_args(argv)
+    if a.small:
+        experiment_small(a.out, epochs=a.epochs)
+    if a.bar:
+        experiment_bar(a.out, nx=a.bar, train_steps=a.train_steps, eval_steps=a.eval_steps, epochs=a.epochs)
+
+
+if __name__ == '__main__':
+    main()

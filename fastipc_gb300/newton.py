@@ -48,7 +48,7 @@ class Timer:
 
 class NewtonIPC:
     def __init__(self, scene, device='cuda:0', pcg_rtol=1e-10, pcg_maxit=200000, eta=0.2, inversion_filter=True,
-                 max_newton=500, max_halvings=64):
+                 max_newton=500, max_halvings=64, pcg_warm_start=False):
         self.scene = scene
         self.device = torch.device(device)
         torch.cuda.set_device(self.device)
@@ -93,6 +93,16 @@ class NewtonIPC:
         self.newton_iters = []
         self.pcg_iters = []
         self.alphas = []
+        # optional PCG initial guess: the direction of the same Newton iteration of the
+        # previous time step (the solution is unchanged up to the PCG tolerance)
+        self.pcg_warm_start = pcg_warm_start
+        self._dir_hist = {}
+        self._newton_k = 0
+        # optional Newton initial guess hook, called as initial_guess(sim, f) after move_nodes
+        # (the reference starts every step from x^n; see fastipc_gb300.learned)
+        self.initial_guess = None
+        # displacement of the step before the last one (v * dt holds the last one)
+        self.dx_prev = torch.zeros_like(self.x)
 
     def close(self):
         if getattr(self, 'ctx', None):
@@ -190,10 +200,17 @@ class NewtonIPC:
         with self.timer('Solve System'):
             self._dirichlet(t)
             it = ctypes.c_int()
-            st = N.lib().fipc_solve_system(self.ctx, dptr(self.fixed, torch.uint8), D(self.pcg_rtol), self.pcg_maxit, 0,
+            guess = self.pcg_warm_start and self._newton_k in self._dir_hist
+            if guess:
+                self.data_sol.copy_(self._dir_hist[self._newton_k])
+                self.data_sol[self.fixed.bool()] = 0.0
+            st = N.lib().fipc_solve_system(self.ctx, dptr(self.fixed, torch.uint8), D(self.pcg_rtol), self.pcg_maxit, int(guess),
                                            dptr(self.data_sol, F64), ctypes.byref(it), self._s())
             check(st, 'solve_system')
             self.pcg_iters.append(it.value)
+            if self.pcg_warm_start:
+                self._dir_hist[self._newton_k] = self.data_sol.clone()
+            self._newton_k += 1
 
     def output_residual(self):
         r = D()
@@ -235,6 +252,9 @@ class NewtonIPC:
         with self.timer('Time Step'):
             self.compute_xn_and_xTilde()
             self.move_nodes(f * self.dt)
+            self._newton_k = 0
+            if self.initial_guess is not None:
+                self.initial_guess(self, f)
             it = 0
             while True:
                 it += 1
@@ -280,6 +300,7 @@ class NewtonIPC:
                     self.alphas.append(alpha)
                     if record is not None:
                         record[-1].update({'E0': E0, 'alpha_ccd': alpha_ccd, 'alpha': alpha, 'E': E})
+            torch.mul(self.v, self.dt, out=self.dx_prev)
             self.compute_v()
         self.newton_iters.append(it)
         return it

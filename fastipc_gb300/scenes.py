@@ -217,3 +217,35 @@ def predeform(scene, amplitude, seed=0):
     scene.x_init = scene.x + d
     scene.meta['predeform'] = amplitude
     return scene
+
+
+def cube_stack(seed, side=0.1, gap=2e-3, min_cubes=1, max_cubes=8, min_hex=3, max_hex=10, ground=(1.0, 0.1, 1.0),
+               jitter=0.1, steps=50):
+    """A seed-drawn stack of 1-8 cubes, each with a seed-drawn 3-10 hexes per side, randomly
+    rotated and stacked along y with at least ``gap`` between bounding spheres, above a fixed
+    ground box; horizontal centres get +-jitter*side.  Sizes run from 168 to 48,006 tets."""
+    rng = np.random.default_rng(seed)
+    k = int(rng.integers(min_cubes, max_cubes + 1))
+    r = np.sqrt(3) * side / 2
+    parts = []
+    y = gap + r
+    for _ in range(k):
+        n = int(rng.integers(min_hex, max_hex + 1))
+        bx, bt = hex_grid(n, n, n, (side, side, side))
+        R = rotation_matrix(rng.normal(size=3), rng.uniform(0, 2 * np.pi))
+        ctr = np.array([rng.uniform(-jitter, jitter) * side, y, rng.uniform(-jitter, jitter) * side])
+        parts.append(((bx - side / 2) @ R.T + ctr, bt))
+        y += 2 * r + gap
+    gx, gy, gz = ground
+    gnd_x, gnd_t = hex_grid(1, 1, 1, (gx, gy, gz))
+    parts.append((gnd_x + np.array([-gx / 2, -gy, -gz / 2]), gnd_t))
+    nv = sum(len(p[0]) for p in parts)
+    mask = np.zeros(nv, dtype=bool)
+    mask[nv - len(gnd_x):] = True
+    return _finish('cube_stack', parts, np.zeros((nv, 3)), _static_dirichlet(mask), steps=steps,
+                   meta={'seed': seed, 'cubes': k})
+
+
+def cube_stacks(n_scenes=512, seed=0, **kw):
+    """``n_scenes`` independent cube stacks with seeds seed, seed+1, ...: the batched workload."""
+    return [cube_stack(seed + i, **kw) for i in range(n_scenes)]

@@ -119,6 +119,62 @@ int fipc_compute_intersection_free_step_size(fipc_ctx* ctx, const double* x, con
 /* check_collision, NEWTON_IPC.py:855-886 */
 int fipc_check_collision(fipc_ctx* ctx, const double* x, int* hit_h, void* stream);
 
+/* ---- learned Newton warm start (no counterpart in the reference) ----------------------------
+ * A per-vertex MLP 55 (padded 64) -> 128 -> 128 -> 128 -> 3 (padded 4), GELU, FP32, parameters
+ * in one flat array (W1 [128][64], b1, W2 [128][128], b2, W3, b3, W4 [4][128], b4). */
+int fipc_mlp_param_count(void);
+/* out [n][4] = MLP(X [n][64]); Z, A: scratch [3][n][128] kept for the backward pass */
+int fipc_mlp_forward(int n, const float* X, const float* params, float* Z, float* A, float* out, void* stream);
+/* grads (params layout) of sum(dout . out) for that forward pass; dA: scratch [2][n][128] */
+int fipc_mlp_backward(int n, const float* X, const float* params, const float* Z, const float* A, const float* dout,
+                      float* grads, float* dA, void* stream);
+/* mean squared error over the first 3 outputs into *loss (device) and its gradient dout [n][4];
+ * part: scratch of ceil(n/256) floats */
+int fipc_mlp_mse(int n, const float* out, const float* target, float* dout, float* part, float* loss, void* stream);
+/* one Adam step, t >= 1 */
+int fipc_mlp_adam(int n_params, float* params, const float* grads, float* m, float* v, float lr, float beta1, float beta2,
+                  float eps, int t, void* stream);
+/* per-vertex inputs X [V][64] at positions x: 16 one-ring relative positions / h, v dt / h,
+ * dx_prev / h (the Python driver passes the displacement of the step before the last one),
+ * min(nearest constraint distance / d-hat, 1) over the lists of the last fipc_find_constraints */
+int fipc_mlp_features(fipc_ctx* ctx, const double* x, const double* v, const double* dx_prev, double h, float* X,
+                      void* stream);
+
+/* ---- batched scenes ---------------------------------------------------------------------- *
+ * S independent scenes (1 <= S <= 1024) in one context, each stepping its own Newton loop of
+ * NEWTON_IPC.py:955-999.  The arrays are the concatenation of the scenes' arrays with global
+ * vertex ids: scene s owns vertices [vert_off[s], vert_off[s+1]), tets [tet_off[s],
+ * tet_off[s+1]) and boundary edges [be_off[s], be_off[s+1]); boundary points and triangles
+ * each lie in one scene.  Every single-scene entry point above accepts a batch context and
+ * then works per scene where the reference's quantity is per scene (hash cell size and kappa
+ * per scene, NEWTON_IPC.py:116-134; keys of different scenes never meet).  The entries below
+ * return one value per scene into device arrays of S. */
+int fipc_batch_create(fipc_ctx** out, int n_scenes, const int* vert_off, const int* tet_off, const int* be_off, int n_verts,
+                      int n_tets, const int* tets, const double* x_rest, const double* lam, const double* mu, double rho,
+                      int n_bp, const int* bp, int n_be, const int* be, int n_bt, const int* bt, double dhat2, double dt);
+/* host copies of the per-scene kappa and inverse hash cell size (arrays of S) */
+int fipc_batch_params(fipc_ctx* ctx, int* n_scenes, double* kappa, double* inv_dx);
+/* compute_energy (NEWTON_IPC.py:515-542) per scene */
+int fipc_batch_compute_energy(fipc_ctx* ctx, const double* x, const double* xtilde, double* energy, void* stream);
+/* output_residual (NEWTON_IPC.py:806-812) per scene: max |sol| over the scene's DOFs */
+int fipc_batch_output_residual(fipc_ctx* ctx, const double* sol, double* residual, void* stream);
+/* compute_intersection_free_step_size (NEWTON_IPC.py:456-468) per scene */
+int fipc_batch_step_size(fipc_ctx* ctx, const double* x, const double* sol, double eta, int inversion, double* alpha,
+                         void* stream);
+/* check_collision (NEWTON_IPC.py:881-886) per scene: hit[s] = 1 when scene s intersects */
+int fipc_batch_check_collision(fipc_ctx* ctx, const double* x, int* hit, void* stream);
+/* apply_sol (NEWTON_IPC.py:792-796) with alpha[scene] */
+int fipc_batch_apply_sol(fipc_ctx* ctx, const double* x_prev, const double* sol, const double* alpha, double* x, void* stream);
+/* solve_system (NEWTON_IPC.py:750-777) for every scene with active[s] != 0 (null: all); the
+ * others get sol = 0.  PCG with per-scene scalars and tolerance (relative to the scene's |rhs|),
+ * persistent kernels over a tile table, iterations replayed as a captured CUDA graph; the
+ * tile shape and grid are chosen by timing at the first call.  iters: device int[S] or null;
+ * *n_failed (host): scenes that hit maxit (status 2 when any did). */
+int fipc_batch_solve_system(fipc_ctx* ctx, const unsigned char* fixed, const unsigned char* active, double rtol, int maxit,
+                            int use_guess, double* sol, int* iters, int* n_failed, void* stream);
+/* the PCG shape the timing picked: rows per tile (= threads per block), grid, tiles, SpMV ms */
+int fipc_batch_pcg_shape(fipc_ctx* ctx, int* tile_rows, int* grid, int* n_tiles, float* spmv_ms);
+
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Time every launch of one kernel with CUDA events on its stream (1 PCG SpMV, 2 PCG update,
  * 3 Neo-Hookean element, 4 barrier rows, 5 elastic assembly; 0 off) and read back the summed
