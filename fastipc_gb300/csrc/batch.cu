@@ -644,6 +644,9 @@ extern "C" int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const in
                                const double* mu, double rho, int n_bp, const int* bp, int n_be, const int* be, int n_bt, const int* bt,
                                double dhat2, double dt);
 extern "C" int fipc_ctx_destroy(fipc_ctx* c);
+namespace fipc {
+int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h);
+}
 
 namespace {
 template <class T>
@@ -685,9 +688,25 @@ int fipc_batch_create(fipc_ctx** out, int n_scenes, const int* vert_off, const i
     }
     for (int k = 0; k < n_bp; ++k)
         if (bp[k] < 0 || bp[k] >= n_verts) return FIPC_ERR_ARGUMENT;
+    // each scene's boundary points, edges and triangles are one run of their list, in scene order
+    std::vector<int> poff(3 * (S + 1), 0);
+    {
+        const int nl[3] = {n_bp, n_be, n_bt};
+        for (int l = 0; l < 3; ++l) {
+            int* o = poff.data() + l * (S + 1);
+            int q = 0;
+            for (int k = 0; k < nl[l]; ++k) {
+                const int sk = vs[l == 0 ? bp[k] : (l == 1 ? be[2 * k] : bt[3 * k])];
+                if (sk < q) return FIPC_ERR_ARGUMENT;
+                while (q < sk) o[++q] = k;
+            }
+            while (q < S) o[++q] = nl[l];
+        }
+    }
     fipc_ctx* c = nullptr;
     int st = fipc_ctx_create(&c, n_verts, n_tets, tets, x_rest, lam, mu, rho, n_bp, bp, n_be, be, n_bt, bt, dhat2, dt);
     if (st) return st;
+    cs_setup(c, 0, nullptr, nullptr);   // the batched PCG preconditions with block-Jacobi
     // per-scene kappa (NEWTON_IPC.py:116-124, x10 at :943) and hash cell (:127-134)
     std::vector<double> mass(n_verts), kap(S), idx(S);
     if (cudaMemcpy(mass.data(), c->mass, 8ll * n_verts, cudaMemcpyDeviceToHost) != cudaSuccess) {
@@ -714,8 +733,9 @@ int fipc_batch_create(fipc_ctx** out, int n_scenes, const int* vert_off, const i
     c->h_toff.assign(tet_off, tet_off + S + 1);
     c->h_kappa = kap;
     c->h_inv_dx = idx;
+    if (c->prim_off) cudaFree(c->prim_off);
     st = upload_vec(&c->v_scene, vs) | upload_vec(&c->voff_d, c->h_voff) | upload_vec(&c->toff_d, c->h_toff) |
-         upload_vec(&c->s_kappa, kap) | upload_vec(&c->s_inv_dx, idx);
+         upload_vec(&c->s_kappa, kap) | upload_vec(&c->s_inv_dx, idx) | upload_vec(&c->prim_off, poff);
     if (st) {
         fipc_ctx_destroy(c);
         return FIPC_ERR_CUDA;

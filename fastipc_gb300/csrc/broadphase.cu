@@ -78,6 +78,10 @@ __global__ void k_cell_count(int mode, int n, const int* __restrict__ prim, cons
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double inv_dx = g.idx(g.scene(prim_vertex(mode, i, prim)));
+    if (mode != 0 && mode != 2 && g.big_edge && g.big_edge[i]) {   // handled by the big-primitive pass
+        cnt[i] = 0;
+        return;
+    }
     v3 lo, hi;
     stored_box(mode, i, prim, x, p, dh, &lo, &hi);
     const C3 a = cell_of(lo, inv_dx), b = cell_of(hi, inv_dx);
@@ -178,6 +182,7 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     const int nu = *nu_p;
+    if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
     const int sc = g.scene(t0);
     const double inv_dx = g.idx(sc);
@@ -207,6 +212,7 @@ __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict_
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbe) return;
     const int nu = *nu_p;
+    if (g.big_edge && g.big_edge[i]) return;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
     const int sc = g.scene(a0);
     const double inv_dx = g.idx(sc);
@@ -244,6 +250,7 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     const int nu = *nu_p;
+    if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
     const int sc = g.scene(t0);
     const double inv_dx = g.idx(sc);
@@ -281,6 +288,7 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbe) return;
     const int nu = *nu_p;
+    if (g.big_edge && g.big_edge[i]) return;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
     const int sc = g.scene(a0);
     const double inv_dx = g.idx(sc);
@@ -329,6 +337,7 @@ __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restric
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     const int nu = *nu_p;
+    if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
     const int sc = g.scene(t0);
     const double inv_dx = g.idx(sc);
@@ -356,6 +365,147 @@ __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restric
                     }
                 }
             }
+}
+
+// ---------------------------------------------------------------- big primitives
+// A triangle or edge whose query box covers more than BIG_CELLS cells (a ground plane meshed
+// with a few large triangles next to finely meshed bodies) would enumerate, or be stored in,
+// thousands of cells.  Such primitives leave the grid: each is tested against every primitive
+// of its own scene with the same narrow phase, so the results are the grid's.
+constexpr long long BIG_CELLS = 256;
+
+__device__ __forceinline__ long long box_cells(v3 lo, v3 hi, double inv_dx) {
+    const C3 a = cell_of(lo, inv_dx), b = cell_of(hi, inv_dx);
+    return (b.x - a.x + 1) * (b.y - a.y + 1) * (b.z - a.z + 1);
+}
+
+// flags and compacted lists; triangle boxes as queried (static or moving bbox), edge boxes as
+// queried (static or moving bbox +- dh).  lists: [0, nbt) triangles, [nbt, nbt + nbe) edges;
+// counts[0..1] (zeroed by the caller)
+__global__ void k_big_flags(int nbt, int nbe, const int* __restrict__ bt, const int* __restrict__ be, const double* __restrict__ x,
+                            const double* __restrict__ p, double dh, SceneGeo g, unsigned char* __restrict__ tri_big,
+                            unsigned char* __restrict__ edge_big, int* __restrict__ list, int* __restrict__ counts) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k < nbt) {
+        const int t0 = bt[3 * k], t1 = bt[3 * k + 1], t2 = bt[3 * k + 2];
+        v3 lo = vmin(vmin(ld3(x, t0), ld3(x, t1)), ld3(x, t2)), hi = vmax(vmax(ld3(x, t0), ld3(x, t1)), ld3(x, t2));
+        if (p) {
+            const v3 A = ld3(x, t0) + ld3(p, t0), B = ld3(x, t1) + ld3(p, t1), C = ld3(x, t2) + ld3(p, t2);
+            lo = vmin(lo, vmin(vmin(A, B), C));
+            hi = vmax(hi, vmax(vmax(A, B), C));
+        }
+        const bool big = box_cells(lo, hi, g.idx(g.scene(t0))) > BIG_CELLS;
+        tri_big[k] = big;
+        if (big) list[atomicAdd(&counts[0], 1)] = k;
+    } else if (k < nbt + nbe) {
+        const int e = k - nbt, a0 = be[2 * e], a1 = be[2 * e + 1];
+        v3 lo = vmin(ld3(x, a0), ld3(x, a1)), hi = vmax(ld3(x, a0), ld3(x, a1));
+        if (p) {
+            const v3 A = ld3(x, a0) + ld3(p, a0), B = ld3(x, a1) + ld3(p, a1);
+            lo = vmin(lo, vmin(A, B));
+            hi = vmax(hi, vmax(A, B));
+        }
+        const v3 d = mk(dh, dh, dh);
+        const bool big = box_cells(lo - d, hi + d, g.idx(g.scene(a0))) > BIG_CELLS;
+        edge_big[e] = big;
+        if (big) list[nbt + atomicAdd(&counts[1], 1)] = e;
+    }
+}
+
+// partners of big primitive q of scene s: lists [off[s], off[s+1]) of its kind
+struct BigArgs {
+    const int *bp, *be, *bt;
+    const int* off;        // [3][S+1]: points, edges, triangles
+    int S;
+    const unsigned char *tri_big, *edge_big;
+    const int* list;       // [nbt + nbe]
+    const int* counts;     // [2]
+    int nbt;
+};
+
+// find_constraints, big triangles against every point of their scene
+__global__ void k_find_pt_big(BigArgs b, const double* __restrict__ x, double dh, double dh2, SceneGeo g, RowSink sink) {
+    for (int q = blockIdx.x; q < b.counts[0]; q += gridDim.x) {
+        const int i = b.list[q];
+        const int t0 = b.bt[3 * i], t1 = b.bt[3 * i + 1], t2 = b.bt[3 * i + 2];
+        const int sc = g.scene(t0);
+        for (int k = b.off[sc] + threadIdx.x; k < b.off[sc + 1]; k += blockDim.x) attempt_pt(x, dh, dh2, b.bp[k], t0, t1, t2, sink);
+    }
+}
+
+// find_constraints, big edges against every edge of their scene (a pair of two big edges once,
+// from its lower index); rows formed with the lower list index first as in the grid pass
+__global__ void k_find_ee_big(BigArgs b, const double* __restrict__ x, const double* __restrict__ x0, double dh, double dh2,
+                              SceneGeo g, RowSink sink) {
+    for (int q = blockIdx.x; q < b.counts[1]; q += gridDim.x) {
+        const int i = b.list[b.nbt + q];
+        const int sc = g.scene(b.be[2 * i]);
+        const int* off = b.off + (b.S + 1);
+        for (int j = off[sc] + threadIdx.x; j < off[sc + 1]; j += blockDim.x) {
+            if (j == i || (b.edge_big[j] && j < i)) continue;
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            attempt_ee(x, x0, dh, dh2, b.be[2 * lo], b.be[2 * lo + 1], b.be[2 * hi], b.be[2 * hi + 1], sink);
+        }
+    }
+}
+
+// CCD filter, big moving triangles against every point of their scene
+__global__ void k_ccd_pt_big(BigArgs b, const double* __restrict__ x, const double* __restrict__ p, double dh, double eta, SceneGeo g,
+                             unsigned long long* __restrict__ alpha) {
+    for (int q = blockIdx.x; q < b.counts[0]; q += gridDim.x) {
+        const int i = b.list[q];
+        const int t0 = b.bt[3 * i], t1 = b.bt[3 * i + 1], t2 = b.bt[3 * i + 2];
+        const int sc = g.scene(t0);
+        const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2), dA = ld3(p, t0), dB = ld3(p, t1), dC = ld3(p, t2);
+        for (int k = b.off[sc] + threadIdx.x; k < b.off[sc + 1]; k += blockDim.x) {
+            const int pp = b.bp[k];
+            if (pp == t0 || pp == t1 || pp == t2) continue;
+            const v3 P = ld3(x, pp), dP = ld3(p, pp);
+            if (!pt_aabb_moving(P, A, B, C, dP, dA, dB, dC, dh)) continue;
+            atomic_min_pos(alpha + (g.vscene ? sc : 0), pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, pt_dist2(P, A, B, C)));
+        }
+    }
+}
+
+// CCD filter, big moving edges against every edge of their scene
+__global__ void k_ccd_ee_big(BigArgs b, const double* __restrict__ x, const double* __restrict__ p, double dh, double eta, SceneGeo g,
+                             unsigned long long* __restrict__ alpha) {
+    for (int q = blockIdx.x; q < b.counts[1]; q += gridDim.x) {
+        const int i = b.list[b.nbt + q];
+        const int sc = g.scene(b.be[2 * i]);
+        const int* off = b.off + (b.S + 1);
+        for (int j = off[sc] + threadIdx.x; j < off[sc + 1]; j += blockDim.x) {
+            if (j == i || (b.edge_big[j] && j < i)) continue;
+            const int lo = i < j ? i : j, hi = i < j ? j : i;
+            const int a0 = b.be[2 * lo], a1 = b.be[2 * lo + 1], b0 = b.be[2 * hi], b1 = b.be[2 * hi + 1];
+            if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) continue;
+            const v3 A0 = ld3(x, a0), A1 = ld3(x, a1), B0 = ld3(x, b0), B1 = ld3(x, b1);
+            const v3 dA0 = ld3(p, a0), dA1 = ld3(p, a1), dB0 = ld3(p, b0), dB1 = ld3(p, b1);
+            if (!ee_aabb_moving(A0, A1, B0, B1, dA0, dA1, dB0, dB1, dh)) continue;
+            atomic_min_pos(alpha + (g.vscene ? sc : 0), ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, ee_dist2(A0, A1, B0, B1)));
+        }
+    }
+}
+
+// intersection check: big triangles against every edge of their scene, big edges against every
+// triangle of their scene that is not big
+__global__ void k_collision_big(BigArgs b, const double* __restrict__ x, SceneGeo g, int* __restrict__ hit) {
+    const int nt = b.counts[0], ne = b.counts[1];
+    for (int q = blockIdx.x; q < nt + ne; q += gridDim.x) {
+        const bool tri = q < nt;
+        const int i = tri ? b.list[q] : b.list[b.nbt + q - nt];
+        const int sc = g.scene(tri ? b.bt[3 * i] : b.be[2 * i]);
+        int* h = hit + (g.vscene ? sc : 0);
+        const int* off = b.off + (tri ? 1 : 2) * (b.S + 1);
+        for (int k = off[sc] + threadIdx.x; k < off[sc + 1]; k += blockDim.x) {
+            if (*(volatile int*)h) break;
+            const int e = tri ? k : i, t = tri ? i : k;
+            if (!tri && b.tri_big[t]) continue;
+            const int t0 = b.bt[3 * t], t1 = b.bt[3 * t + 1], t2 = b.bt[3 * t + 2], a0 = b.be[2 * e], a1 = b.be[2 * e + 1];
+            if (a0 == t0 || a0 == t1 || a0 == t2 || a1 == t0 || a1 == t1 || a1 == t2) continue;
+            if (seg_tri(ld3(x, a0), ld3(x, a1), ld3(x, t0), ld3(x, t1), ld3(x, t2))) atomicOr(h, 1);
+        }
+    }
 }
 
 // ---------------------------------------------------------------- row canonicalisation
@@ -416,8 +566,40 @@ static SceneGeo geo(const fipc_ctx* c) {
     return g;
 }
 
+// flag the big triangles and edges for positions x (+ direction p when moving) and return the
+// scene lookup that carries the flags; *b gets the lists for the big-primitive kernels
+static int big_prepare(fipc_ctx* c, const double* x, const double* p, SceneGeo* g, BigArgs* b, cudaStream_t s) {
+    *g = geo(c);
+    const int n = c->nBT + c->nBE;
+    if (c->big_flags.ensure((size_t)n + 16) || c->big_list.ensure(4ll * (n + 2) + 16)) return FIPC_ERR_CUDA;
+    unsigned char* tri_big = c->big_flags.as<unsigned char>();
+    int* list = c->big_list.as<int>();
+    int* counts = list + n;
+    FIPC_CUDA(cudaMemsetAsync(counts, 0, 2 * sizeof(int), s));
+    if (n > 0) {
+        k_big_flags<<<nblk(n, 256), 256, 0, s>>>(c->nBT, c->nBE, c->bt, c->be, x, p, c->dhat, *g, tri_big, tri_big + c->nBT, list,
+                                                 counts);
+        FIPC_LAUNCHED();
+    }
+    g->big_tri = tri_big;
+    g->big_edge = tri_big + c->nBT;
+    b->bp = c->bp;
+    b->be = c->be;
+    b->bt = c->bt;
+    b->off = c->prim_off;
+    b->S = c->n_scenes;
+    b->tri_big = g->big_tri;
+    b->edge_big = g->big_edge;
+    b->list = list;
+    b->counts = counts;
+    b->nbt = c->nBT;
+    return FIPC_OK;
+}
+constexpr int BIG_GRID = 304, BIG_THREADS = 128;
+
 // build grid g over n stored primitives; scal: device int scratch (overflow flag at [0])
-int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const double* x, const double* p, cudaStream_t s) {
+int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const double* x, const double* p, const SceneGeo& sg,
+               cudaStream_t s) {
     g.n_entries = 0;
     g.n_unique = 0;
     if (g.counts.ensure(sizeof(long long) * (n + 1)) || g.offsets.ensure(sizeof(long long) * (n + 1)) ||
@@ -426,7 +608,7 @@ int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const dou
     FIPC_CUDA(cudaMemsetAsync(g.ncells.p, 0, sizeof(int) * 2, s));
     if (n == 0) return FIPC_OK;
     int* ovf = g.ncells.as<int>() + 1;
-    k_cell_count<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, geo(c), g.counts.as<long long>(), ovf);
+    k_cell_count<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, sg, g.counts.as<long long>(), ovf);
     FIPC_LAUNCHED();
     long long* cnt = g.counts.as<long long>();
     long long* off = g.offsets.as<long long>();
@@ -446,7 +628,7 @@ int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const dou
     if (g.keys.ensure(8 * total) || g.keys_alt.ensure(8 * total) || g.ids.ensure(4 * total) || g.ids_alt.ensure(4 * total) ||
         g.ukeys.ensure(8 * total) || g.ustart.ensure(4 * (total + 1)) || g.tmp.ensure(4 * (total + 1)))
         return FIPC_ERR_CUDA;
-    k_cell_emit<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, geo(c), off, cnt, g.keys.as<unsigned long long>(),
+    k_cell_emit<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, sg, off, cnt, g.keys.as<unsigned long long>(),
                                              g.ids.as<int>());
     FIPC_LAUNCHED();
     cub::DoubleBuffer<unsigned long long> kb(g.keys.as<unsigned long long>(), g.keys_alt.as<unsigned long long>());
@@ -535,20 +717,32 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         for (int t = 0; t < N_TYPES; ++t) sink.rows[t] = c->rows[t].as<int4>();
         sink.counts = c->d_counts;
         sink.cap = c->cap;
-        int st = build_grid(c, c->gp, 0, c->nBP, c->bp, x, nullptr, s);
+        SceneGeo sg;
+        BigArgs bg;
+        int st = big_prepare(c, x, nullptr, &sg, &bg, s);
+        if (st) return st;
+        st = build_grid(c, c->gp, 0, c->nBP, c->bp, x, nullptr, sg, s);
         if (st) return st;
         if (c->gp.n_entries > 0 && c->nBT > 0) {
-            k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, geo(c),
+            k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, sg,
                                                          c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
                                                          c->gp.ncells.as<int>(), c->gp.ids.as<int>(), sink);
             FIPC_LAUNCHED();
         }
-        st = build_grid(c, c->ge, 1, c->nBE, c->be, x, nullptr, s);
+        if (c->nBT > 0 && c->nBP > 0) {
+            k_find_pt_big<<<BIG_GRID, BIG_THREADS, 0, s>>>(bg, x, c->dhat, c->dhat2, sg, sink);
+            FIPC_LAUNCHED();
+        }
+        st = build_grid(c, c->ge, 1, c->nBE, c->be, x, nullptr, sg, s);
         if (st) return st;
         if (c->ge.n_entries > 0) {
-            k_find_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, geo(c),
+            k_find_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, sg,
                                                          c->ge.ukeys.as<unsigned long long>(), c->ge.ustart.as<int>(),
                                                          c->ge.ncells.as<int>(), c->ge.ids.as<int>(), sink);
+            FIPC_LAUNCHED();
+        }
+        if (c->nBE > 1) {
+            k_find_ee_big<<<BIG_GRID, BIG_THREADS, 0, s>>>(bg, x, c->x0, c->dhat, c->dhat2, sg, sink);
             FIPC_LAUNCHED();
         }
         FIPC_CUDA(cudaGetLastError());
@@ -569,23 +763,35 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
 // compute_intersection_free_step_size (NEWTON_IPC.py:456-468): the launches, min'd into
 // slots (one double per scene, preset to 1.0 by the caller)
 int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool inversion, unsigned long long* slot, cudaStream_t s) {
-    int st = build_grid(c, c->gp, 2, c->nBP, c->bp, x, p, s);
+    SceneGeo sg;
+    BigArgs bg;
+    int st = big_prepare(c, x, p, &sg, &bg, s);
+    if (st) return st;
+    st = build_grid(c, c->gp, 2, c->nBP, c->bp, x, p, sg, s);
     if (st) return st;
     if (c->gp.n_entries > 0 && c->nBT > 0) {
-        k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, geo(c), eta,
+        k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, sg, eta,
                                                     c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
                                                     c->gp.ncells.as<int>(), c->gp.ids.as<int>(), slot);
         FIPC_LAUNCHED();
     }
-    st = build_grid(c, c->ge, 3, c->nBE, c->be, x, p, s);
+    if (c->nBT > 0 && c->nBP > 0) {
+        k_ccd_pt_big<<<BIG_GRID, BIG_THREADS, 0, s>>>(bg, x, p, c->dhat, eta, sg, slot);
+        FIPC_LAUNCHED();
+    }
+    st = build_grid(c, c->ge, 3, c->nBE, c->be, x, p, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0) {
-        k_ccd_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, geo(c), eta, c->ge.ukeys.as<unsigned long long>(),
+        k_ccd_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, c->ge.ukeys.as<unsigned long long>(),
                                                     c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), slot);
         FIPC_LAUNCHED();
     }
+    if (c->nBE > 1) {
+        k_ccd_ee_big<<<BIG_GRID, BIG_THREADS, 0, s>>>(bg, x, p, c->dhat, eta, sg, slot);
+        FIPC_LAUNCHED();
+    }
     if (inversion && c->nT > 0) {
-        k_ccd_inversion<<<nblk(c->nT, 128), 128, 0, s>>>(c->nT, (const int4*)c->tets, x, p, eta, geo(c), slot);
+        k_ccd_inversion<<<nblk(c->nT, 128), 128, 0, s>>>(c->nT, (const int4*)c->tets, x, p, eta, sg, slot);
         FIPC_LAUNCHED();
     }
     FIPC_CUDA(cudaGetLastError());
@@ -608,11 +814,19 @@ int ccd_step(fipc_ctx* c, const double* x, const double* p, double eta, bool inv
 // check_collision_3d (NEWTON_IPC.py:881-886): the launches, or'd into hit (one int per scene,
 // zeroed by the caller)
 int collision_launch(fipc_ctx* c, const double* x, int* hit, cudaStream_t s) {
-    int st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, s);
+    SceneGeo sg;
+    BigArgs bg;
+    int st = big_prepare(c, x, nullptr, &sg, &bg, s);
+    if (st) return st;
+    st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0 && c->nBT > 0) {
-        k_collision<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, geo(c), c->ge.ukeys.as<unsigned long long>(),
+        k_collision<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, sg, c->ge.ukeys.as<unsigned long long>(),
                                                        c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), hit);
+        FIPC_LAUNCHED();
+    }
+    if (c->nBT > 0 && c->nBE > 0) {
+        k_collision_big<<<BIG_GRID, BIG_THREADS, 0, s>>>(bg, x, sg, hit);
         FIPC_LAUNCHED();
     }
     FIPC_CUDA(cudaGetLastError());

@@ -25,6 +25,15 @@ int launch_energy(const fipc_ctx* c, const double* x, const double* xt, const in
                   double* out, cudaStream_t s);
 int launch_absmax(int n, const double* p, double* part, double* out, cudaStream_t s);
 void free_batch(fipc_ctx* c);
+int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h);
+void cs_free(fipc_ctx* c);
+// default aggregate size of the two-level preconditioner: 2048 vertices, larger when needed to
+// keep the dense coarse matrix at most 6 x 512 square
+int default_agg_rows(int n_verts) {
+    const int per = (n_verts + 511) / 512;
+    const int a = ((per + 127) / 128) * 128;
+    return a > 2048 ? a : 2048;
+}
 }  // namespace fipc
 
 using namespace fipc;
@@ -46,15 +55,16 @@ double det3h(const double* A) {
 
 void free_ctx(fipc_ctx* c) {
     free_batch(c);
+    cs_free(c);
     void* ptrs[] = {c->tets, c->bp, c->be, c->bt, c->dminv, c->vol, c->lam, c->mu, c->mass, c->x0, c->row_ptr, c->col_idx,
                     c->up_pos, c->up_tpos, c->up_row, c->up_cptr, c->up_contrib, c->vt_ptr, c->vt_list, c->elem_g, c->elem_H,
                     c->bsr_val, c->rhs, c->d_counts, c->diag_pos, c->sell_off, c->sell_col, c->row_len, c->bsr2sell,
-                    c->up_spos, c->up_tspos, c->diag_spos, c->sell_val};
+                    c->up_spos, c->up_tspos, c->diag_spos, c->sell_val, c->prim_off};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     for (int t = 0; t < N_TYPES; ++t) c->rows[t].release();
     DBuf* bufs[] = {&c->rows_tmp, &c->sort_keys, &c->sort_keys_alt, &c->sort_vals, &c->sort_vals_alt, &c->flags, &c->scan,
-                    &c->cub_tmp, &c->c_g, &c->c_H, &c->c_keys, &c->c_keys_alt, &c->c_vals, &c->c_vals_alt, &c->c_ukeys,
+                    &c->cub_tmp, &c->big_flags, &c->big_list, &c->c_g, &c->c_H, &c->c_keys, &c->c_keys_alt, &c->c_vals, &c->c_vals_alt, &c->c_ukeys,
                     &c->c_ucount, &c->c_ustart, &c->c_val, &c->c_rowptr, &c->c_col, &c->pcg_vec, &c->pcg_part, &c->scal, &c->red, &c->mlp_dist};
     for (DBuf* b : bufs) b->release();
     Grid* gs[] = {&c->gp, &c->ge};
@@ -262,6 +272,10 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
     st |= upload(&c->up_spos, up_spos.data(), up_spos.size());
     st |= upload(&c->up_tspos, up_tspos.data(), up_tspos.size());
     st |= upload(&c->diag_spos, diag_spos.data(), diag_spos.size());
+    {
+        const int off[6] = {0, n_bp, 0, n_be, 0, n_bt};   // one scene: whole boundary lists
+        st |= upload(&c->prim_off, off, 6);
+    }
     c->n_slices = n_slices;
     c->n_slots = n_slots;
     c->nnzb = (int)nnzb;
@@ -277,6 +291,7 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
             st = FIPC_ERR_CUDA;
     }
     if (st == FIPC_OK) st = ensure_row_capacity(c, 4096);
+    if (st == FIPC_OK) st = cs_setup(c, default_agg_rows(n_verts), row_ptr.data(), col_idx.data());
     if (st != FIPC_OK) {
         free_ctx(c);
         return FIPC_ERR_CUDA;
@@ -289,6 +304,22 @@ int fipc_ctx_destroy(fipc_ctx* c) {
     if (!c) return FIPC_ERR_ARGUMENT;
     cudaDeviceSynchronize();
     free_ctx(c);
+    return FIPC_OK;
+}
+
+int fipc_ctx_set_preconditioner(fipc_ctx* c, int agg_rows) {
+    if (!c || agg_rows < 0 || agg_rows % 128) return FIPC_ERR_ARGUMENT;
+    std::vector<int> rp(c->nV + 1), ci(c->nnzb);
+    if (cudaMemcpy(rp.data(), c->row_ptr, 4ll * (c->nV + 1), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(ci.data(), c->col_idx, 4ll * c->nnzb, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return FIPC_ERR_CUDA;
+    return cs_setup(c, agg_rows, rp.data(), ci.data());
+}
+
+int fipc_ctx_preconditioner(fipc_ctx* c, int* agg_rows, int* n_coarse) {
+    if (!c) return FIPC_ERR_ARGUMENT;
+    if (agg_rows) *agg_rows = c->cs_agg_rows;
+    if (n_coarse) *n_coarse = 6 * c->cs_n_agg;
     return FIPC_OK;
 }
 

@@ -1,0 +1,300 @@
+// Two-level preconditioner for the PCG direction solve: block-Jacobi plus a coarse correction
+// on the six rigid-body modes (three translations, three rotations) of each aggregate of
+// consecutive vertices,
+//     M^-1 r = D^-1 r + P Ac^-1 P^T r,   Ac = P^T A P,   P_i = [I, -[d_i]x]  (3 x 6),
+// with d_i the offset of vertex i from its aggregate's centroid and Dirichlet rows of P zero.
+// Both terms are symmetric positive (semi)definite, so CG keeps converging to the solution of
+// the reference's system (NEWTON_IPC.py:750-777); only the iteration count changes.  Long or
+// stacked bodies have low-frequency modes that block-Jacobi resolves only one mesh layer per
+// iteration; the coarse space removes them.
+//
+// Aggregates are runs of cs_agg_rows vertices, a multiple of the PCG block, so each PCG block
+// restricts its residuals into its own aggregate with one fixed-order block sum.  Ac is built
+// from the elastic + inertia blocks (one CTA per coupled aggregate pair, fixed-order sums),
+// inverted densely in place by Gauss-Jordan in one cooperative launch, and applied as a dense
+// matrix-vector product per PCG iteration.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "ctx.cuh"
+#include "pcg.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace fipc {
+
+static inline int nblk_c(long long n, int b) { return (int)((n + b - 1) / b); }
+
+// one CTA per aggregate: centroid of its vertices (fixed order), then d_i = x_i - centroid
+constexpr int CS_THREADS = 128;
+__global__ void __launch_bounds__(CS_THREADS) k_cs_offsets(int nV, int agg_rows, const double* __restrict__ x, double* __restrict__ d) {
+    __shared__ double sh[3][CS_THREADS];
+    const int a = blockIdx.x, i0 = a * agg_rows, i1 = min(nV, i0 + agg_rows);
+    double c[3] = {0.0, 0.0, 0.0};
+    for (int i = i0 + threadIdx.x; i < i1; i += CS_THREADS)
+        for (int k = 0; k < 3; ++k) c[k] += x[3 * (size_t)i + k];
+    for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] = c[k];
+    __syncthreads();
+    for (int s = CS_THREADS / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s)
+            for (int k = 0; k < 3; ++k) sh[k][threadIdx.x] += sh[k][threadIdx.x + s];
+        __syncthreads();
+    }
+    const double inv = 1.0 / (double)(i1 - i0);
+    const double cx = sh[0][0] * inv, cy = sh[1][0] * inv, cz = sh[2][0] * inv;
+    for (int i = i0 + threadIdx.x; i < i1; i += CS_THREADS) {
+        d[3 * (size_t)i] = x[3 * (size_t)i] - cx;
+        d[3 * (size_t)i + 1] = x[3 * (size_t)i + 1] - cy;
+        d[3 * (size_t)i + 2] = x[3 * (size_t)i + 2] - cz;
+    }
+}
+
+// C += P_i^T B P_j for the 3x3 block B (row-major, entries at B[32 * e])
+__device__ __forceinline__ void add_coarse_block(double (&C)[36], const double* __restrict__ B, const double (&di)[3],
+                                                 const double (&dj)[3]) {
+    double b[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e) b[e] = __ldg(B + 32 * e);
+    // S(d) v = d x v;  BS = B S(dj), SB = S(di) B, SBS = S(di) B S(dj)
+    const double Sj[9] = {0.0, -dj[2], dj[1], dj[2], 0.0, -dj[0], -dj[1], dj[0], 0.0};
+    const double Si[9] = {0.0, -di[2], di[1], di[2], 0.0, -di[0], -di[1], di[0], 0.0};
+    double BS[9], SB[9];
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            BS[3 * r + c] = b[3 * r] * Sj[c] + b[3 * r + 1] * Sj[3 + c] + b[3 * r + 2] * Sj[6 + c];
+            SB[3 * r + c] = Si[3 * r] * b[c] + Si[3 * r + 1] * b[3 + c] + Si[3 * r + 2] * b[6 + c];
+        }
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const double sbs = Si[3 * r] * BS[c] + Si[3 * r + 1] * BS[3 + c] + Si[3 * r + 2] * BS[6 + c];
+            C[6 * r + c] += b[3 * r + c];
+            C[6 * r + 3 + c] -= BS[3 * r + c];
+            C[6 * (3 + r) + c] += SB[3 * r + c];
+            C[6 * (3 + r) + 3 + c] -= sbs;
+        }
+}
+
+// one CTA per coupled aggregate pair (I, J): the 6x6 block Ac[I][J] = sum over free i in I and
+// free j in J of P_i^T A_ij P_j (elastic + inertia blocks), fixed-order sums, into dense Ac
+__global__ void __launch_bounds__(CS_THREADS) k_cs_build(int nV, int agg_rows, int n, const int* __restrict__ pairs,
+                                                         const int* __restrict__ soff, const int* __restrict__ scol,
+                                                         const int* __restrict__ rlen, const double* __restrict__ sval,
+                                                         const unsigned char* __restrict__ fixed, const double* __restrict__ d,
+                                                         double* __restrict__ Ac) {
+    __shared__ double sh[36][CS_THREADS / 32];
+    const int I = pairs[2 * blockIdx.x], J = pairs[2 * blockIdx.x + 1];
+    const int i0 = I * agg_rows, i1 = min(nV, i0 + agg_rows), j0 = J * agg_rows, j1 = min(nV, j0 + agg_rows);
+    double C[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) C[e] = 0.0;
+    for (int i = i0 + threadIdx.x; i < i1; i += CS_THREADS) {
+        if (fixed[i]) continue;
+        const double di[3] = {d[3 * (size_t)i], d[3 * (size_t)i + 1], d[3 * (size_t)i + 2]};
+        const int sl = i >> 5, lane = i & 31, base = soff[sl], len = rlen[i];
+        for (int k = 0; k < len; ++k) {
+            const size_t slot = (size_t)(base + k);
+            const int j = __ldg(scol + slot * 32 + lane);
+            if (j < j0 || j >= j1 || fixed[j]) continue;
+            const double dj[3] = {d[3 * (size_t)j], d[3 * (size_t)j + 1], d[3 * (size_t)j + 2]};
+            add_coarse_block(C, sval + slot * 288 + lane, di, dj);
+        }
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int e = 0; e < 36; ++e) {
+        double v = C[e];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[e][wid] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 36) {
+        double t = 0.0;
+        for (int w = 0; w < CS_THREADS / 32; ++w) t += sh[threadIdx.x][w];
+        const int r = threadIdx.x / 6, c = threadIdx.x % 6;
+        Ac[(size_t)(6 * I + r) * n + 6 * J + c] = t;
+    }
+}
+
+// zero diagonals (modes without free vertices: their rows and columns are zero) become 1; the
+// others get a 1e-12 relative shift that keeps nearly degenerate rotation modes invertible
+__global__ void k_cs_regularize(int n, double* __restrict__ Ac) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    double* dk = Ac + (size_t)k * n + k;
+    *dk = *dk > 0.0 ? *dk * (1.0 + 1e-12) : 1.0;
+}
+
+// in-place Gauss-Jordan inverse of the SPD matrix A (n x n, no pivoting needed); one
+// cooperative launch, one grid barrier per pivot.  buf: 4n doubles (pivot row / column, double
+// buffered: the threads that write row and column k+1 during step k stage them for step k+1)
+__global__ void k_cs_gauss_jordan(int n, double* __restrict__ A, double* __restrict__ buf) {
+    cg::grid_group grid = cg::this_grid();
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x, nthr = (long long)gridDim.x * blockDim.x;
+    const long long nn = (long long)n * n;
+    double* bc[2] = {buf, buf + 2 * n};
+    double* br[2] = {buf + n, buf + 3 * n};
+    for (long long e = tid; e < n; e += nthr) {
+        bc[0][e] = A[e * n];
+        br[0][e] = A[e];
+    }
+    grid.sync();
+    for (int k = 0; k < n; ++k) {
+        const double* col = bc[k & 1];
+        const double* row = br[k & 1];
+        double* ncol = bc[(k + 1) & 1];
+        double* nrow = br[(k + 1) & 1];
+        const double inv = 1.0 / row[k];
+        for (long long e = tid; e < nn; e += nthr) {
+            const int i = (int)(e / n), j = (int)(e - (long long)i * n);
+            double v;
+            if (i == k) v = (j == k) ? inv : row[j] * inv;
+            else if (j == k) v = -col[i] * inv;
+            else v = A[e] - col[i] * row[j] * inv;
+            A[e] = v;
+            if (j == k + 1) ncol[i] = v;
+            if (i == k + 1) nrow[j] = v;
+        }
+        grid.sync();
+    }
+}
+
+// y = Ac^-1 g with g_I = sum of the restriction partials of aggregate I's PCG blocks (fixed
+// order); every CTA forms g in shared memory, then one warp per row
+constexpr int CS_MV_THREADS = 256;
+__global__ void __launch_bounds__(CS_MV_THREADS) k_cs_coarse(PCGArgs a, int n, int nb, const double* __restrict__ Ainv) {
+    extern __shared__ double g[];
+    if (*(volatile int*)&a.flag[0]) return;
+    for (int q = threadIdx.x; q < n; q += CS_MV_THREADS) {
+        const int I = q / 6, c = q % 6;
+        const int b0 = I * a.cs_blocks, b1 = min(nb, b0 + a.cs_blocks);
+        double t = 0.0;
+        for (int b = b0; b < b1; ++b) t += a.cs_part[6 * (size_t)b + c];
+        g[q] = t;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warps = CS_MV_THREADS / 32;
+    for (int row = blockIdx.x * warps + (threadIdx.x >> 5); row < n; row += gridDim.x * warps) {
+        const double* Ar = Ainv + (size_t)row * n;
+        double t = 0.0;
+        for (int j = lane; j < n; j += 32) t += Ar[j] * g[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) a.cs_y[row] = t;
+    }
+}
+
+// u_i += P_i y_I = y_t + y_w x d_i on free vertices
+__global__ void __launch_bounds__(PCG_THREADS) k_cs_prolong(PCGArgs a, int agg_rows) {
+    if (*(volatile int*)&a.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nV || a.fixed[i]) return;
+    const double* y = a.cs_y + 6 * (size_t)(i / agg_rows);
+    const double dx = a.cs_d[3 * (size_t)i], dy = a.cs_d[3 * (size_t)i + 1], dz = a.cs_d[3 * (size_t)i + 2];
+    a.u[4 * (size_t)i] += y[0] + (y[4] * dz - y[5] * dy);
+    a.u[4 * (size_t)i + 1] += y[1] + (y[5] * dx - y[3] * dz);
+    a.u[4 * (size_t)i + 2] += y[2] + (y[3] * dy - y[4] * dx);
+}
+
+// ---------------------------------------------------------------- host side
+// aggregate pairs coupled by the static pattern (host, at context creation or on a change of
+// the aggregate size)
+int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h) {
+    if (c->cs_pairs) cudaFree(c->cs_pairs);
+    c->cs_pairs = nullptr;
+    c->cs_agg_rows = 0;
+    c->cs_n_agg = 0;
+    c->cs_n_pairs = 0;
+    if (agg_rows <= 0) return FIPC_OK;
+    if (agg_rows % PCG_THREADS) return FIPC_ERR_ARGUMENT;
+    const int na = (c->nV + agg_rows - 1) / agg_rows;
+    if (na > 1024) return FIPC_ERR_ARGUMENT;   // dense coarse matrix of at most 6144^2
+    std::vector<unsigned long long> keys;
+    for (int i = 0; i < c->nV; ++i)
+        for (int k = row_ptr_h[i]; k < row_ptr_h[i + 1]; ++k)
+            keys.push_back(((unsigned long long)(i / agg_rows) << 32) | (unsigned)(col_idx_h[k] / agg_rows));
+    std::sort(keys.begin(), keys.end());
+    keys.erase(std::unique(keys.begin(), keys.end()), keys.end());
+    std::vector<int> pairs(2 * keys.size());
+    for (size_t q = 0; q < keys.size(); ++q) {
+        pairs[2 * q] = (int)(keys[q] >> 32);
+        pairs[2 * q + 1] = (int)(keys[q] & 0xffffffffu);
+    }
+    if (cudaMalloc((void**)&c->cs_pairs, sizeof(int) * pairs.size()) != cudaSuccess) return FIPC_ERR_CUDA;
+    if (cudaMemcpy(c->cs_pairs, pairs.data(), sizeof(int) * pairs.size(), cudaMemcpyHostToDevice) != cudaSuccess) return FIPC_ERR_CUDA;
+    c->cs_agg_rows = agg_rows;
+    c->cs_n_agg = na;
+    c->cs_n_pairs = (int)keys.size();
+    return FIPC_OK;
+}
+
+// offsets from the aggregate centroids at the Newton iterate x (called by the assembly)
+int cs_offsets(fipc_ctx* c, const double* x, cudaStream_t s) {
+    if (!c->cs_agg_rows) return FIPC_OK;
+    if (c->cs_d.ensure(24ll * c->nV)) return FIPC_ERR_CUDA;
+    k_cs_offsets<<<c->cs_n_agg, CS_THREADS, 0, s>>>(c->nV, c->cs_agg_rows, x, c->cs_d.as<double>());
+    FIPC_LAUNCHED();
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+
+// Ac^-1 for the assembled system and the Dirichlet mask; fills the coarse fields of a
+int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t s) {
+    a.cs_blocks = 0;
+    if (!c->cs_agg_rows) return FIPC_OK;
+    const int n = 6 * c->cs_n_agg, nb = nblk_c(c->nV, PCG_THREADS);
+    if (c->cs_Ac.ensure(8ll * n * n) || c->cs_buf.ensure(8ll * 4 * n) || c->cs_part.ensure(48ll * nb) || c->cs_y.ensure(8ll * n))
+        return FIPC_ERR_CUDA;
+    double* Ac = c->cs_Ac.as<double>();
+    FIPC_CUDA(cudaMemsetAsync(Ac, 0, 8ll * n * n, s));
+    k_cs_build<<<c->cs_n_pairs, CS_THREADS, 0, s>>>(c->nV, c->cs_agg_rows, n, c->cs_pairs, c->sell_off, c->sell_col, c->row_len,
+                                                    c->sell_val, fixed, c->cs_d.as<double>(), Ac);
+    FIPC_LAUNCHED();
+    k_cs_regularize<<<nblk_c(n, 128), 128, 0, s>>>(n, Ac);
+    FIPC_LAUNCHED();
+    int dev = 0, nsm = 0, per = 0;
+    FIPC_CUDA(cudaGetDevice(&dev));
+    FIPC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    FIPC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cs_gauss_jordan, 256, 0));
+    if (per < 1) return FIPC_ERR_CUDA;
+    int grid = nsm * (per < 2 ? per : 2);
+    const long long need = ((long long)n * n + 255) / 256;
+    if (grid > need) grid = (int)(need > 0 ? need : 1);
+    int nn = n;
+    double* buf = c->cs_buf.as<double>();
+    void* args[] = {&nn, &Ac, &buf};
+    FIPC_CUDA(cudaLaunchCooperativeKernel((const void*)k_cs_gauss_jordan, dim3(grid), dim3(256), args, 0, s));
+    FIPC_LAUNCHED();
+    a.cs_blocks = c->cs_agg_rows / PCG_THREADS;
+    a.cs_d = c->cs_d.as<double>();
+    a.cs_part = c->cs_part.as<double>();
+    a.cs_y = c->cs_y.as<double>();
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+
+// the coarse correction u += P Ac^-1 P^T r for the restriction partials the last PCG kernel wrote
+void cs_apply(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s) {
+    const int n = 6 * c->cs_n_agg, nb = nblk_c(c->nV, PCG_THREADS);
+    const int grid = nblk_c(n, CS_MV_THREADS / 32);
+    k_cs_coarse<<<grid, CS_MV_THREADS, 8 * n, s>>>(a, n, nb, c->cs_Ac.as<double>());
+    FIPC_LAUNCHED();
+    k_cs_prolong<<<nb, PCG_THREADS, 0, s>>>(a, c->cs_agg_rows);
+    FIPC_LAUNCHED();
+}
+
+void cs_free(fipc_ctx* c) {
+    if (c->cs_pairs) cudaFree(c->cs_pairs);
+    c->cs_pairs = nullptr;
+    DBuf* bufs[] = {&c->cs_d, &c->cs_Ac, &c->cs_diag, &c->cs_buf, &c->cs_part, &c->cs_y};
+    for (DBuf* b : bufs) b->release();
+}
+
+}  // namespace fipc

@@ -90,6 +90,11 @@ struct fipc_ctx_impl {
     int c_rows = 0, c_nnzb = 0;
     // PCG
     DBuf pcg_vec, pcg_part;
+    // two-level preconditioner: block-Jacobi plus a coarse space of the six rigid-body modes of
+    // each aggregate of cs_agg_rows consecutive vertices (0: block-Jacobi only)
+    int cs_agg_rows = 0, cs_n_agg = 0, cs_n_pairs = 0;
+    int* cs_pairs = nullptr;              // [cs_n_pairs][2] aggregate pairs coupled by the pattern
+    DBuf cs_d, cs_Ac, cs_diag, cs_buf, cs_part, cs_y;
     // grids
     Grid gp, ge;
     // small device scalars: [0] alpha bits, [1] hit flag, reductions ...
@@ -102,6 +107,10 @@ struct fipc_ctx_impl {
     int *v_scene = nullptr, *voff_d = nullptr, *toff_d = nullptr;
     double *s_kappa = nullptr, *s_inv_dx = nullptr;
     std::vector<int> h_voff, h_toff;
+    // boundary lists of scene s: points [prim_off[0][s], prim_off[0][s+1]), edges [1], triangles
+    // [2] (device, 3 x (n_scenes + 1)); big-primitive flags and lists of the spatial hash
+    int* prim_off = nullptr;
+    DBuf big_flags, big_list;
     std::vector<double> h_kappa, h_inv_dx;
     // batched PCG: tiles of consecutive rows inside one scene
     int n_tiles = 0, tile_rows = 0, pcg_grid = 0;
@@ -118,6 +127,10 @@ struct SceneGeo {
     const int* vscene = nullptr;
     const double* inv_dx_s = nullptr;
     double inv_dx = 1.0;
+    // primitives whose query box covers more than BIG_CELLS cells: tested against every
+    // primitive of their scene instead of through the grid (null: none)
+    const unsigned char* big_tri = nullptr;
+    const unsigned char* big_edge = nullptr;
 #if defined(__CUDACC__)
     __device__ __forceinline__ int scene(int v) const { return vscene ? __ldg(vscene + v) : 0; }
     __device__ __forceinline__ double idx(int s) const { return vscene ? __ldg(inv_dx_s + s) : inv_dx; }

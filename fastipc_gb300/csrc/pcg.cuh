@@ -18,6 +18,11 @@ struct PCGArgs {
     double* part;                    // [3][nblk]
     double* sc;                      // scalars, see SC_*
     int* flag;                       // [0] done, [1] iterations, [2] ticket
+    // coarse space (cs_blocks = PCG blocks per aggregate; 0: block-Jacobi only)
+    int cs_blocks;
+    const double* cs_d;              // [V][3] vertex offset from its aggregate's centroid
+    double* cs_part;                 // [nblk][6] per-block restriction (force, torque) of r
+    double* cs_y;                    // [6 n_agg] coarse correction
 };
 enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
 constexpr int PCG_THREADS = 128;
@@ -85,6 +90,36 @@ __device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double*
         y0 = fma(B[0], v0, fma(B[1], v1, fma(B[2], v2, y0)));
         y1 = fma(B[3], v0, fma(B[4], v1, fma(B[5], v2, y1)));
         y2 = fma(B[6], v0, fma(B[7], v1, fma(B[8], v2, y2)));
+    }
+}
+
+// restriction of one block's residuals onto the rigid-body modes of its aggregate:
+// sum over rows of (r_i, d_i x r_i) into cs_part[block] (fixed shuffle / shared order)
+__device__ __forceinline__ void block_restrict(const PCGArgs& a, bool valid, int i, const double (&r)[3]) {
+    __shared__ double sh[6][PCG_THREADS / 32];
+    double v[6] = {0, 0, 0, 0, 0, 0};
+    if (valid) {
+        const double dx = a.cs_d[3 * (size_t)i], dy = a.cs_d[3 * (size_t)i + 1], dz = a.cs_d[3 * (size_t)i + 2];
+        v[0] = r[0];
+        v[1] = r[1];
+        v[2] = r[2];
+        v[3] = dy * r[2] - dz * r[1];
+        v[4] = dz * r[0] - dx * r[2];
+        v[5] = dx * r[1] - dy * r[0];
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        double x = v[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[c][wid] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        double t = 0.0;
+        for (int k = 0; k < PCG_THREADS / 32; ++k) t += sh[threadIdx.x][k];
+        a.cs_part[6 * (size_t)blockIdx.x + threadIdx.x] = t;
     }
 }
 

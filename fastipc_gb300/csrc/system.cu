@@ -233,7 +233,7 @@ __device__ __forceinline__ void final_sums(const PCGArgs& a, double (&out)[NV]) 
 // residual of the initial guess, block-Jacobi inverse, u = M^-1 r; partials of (r,r)
 __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const double* __restrict__ rhs, double rtol) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double rr = 0.0, bb = 0.0;
+    double rr = 0.0, bb = 0.0, r3[3] = {0.0, 0.0, 0.0};
     if (i < a.nV) {
         double Mi[9];
         const bool fx = a.fixed[i] != 0;
@@ -253,7 +253,11 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const doub
         }
         a.u[4 * i + 3] = 0.0;
         rr = r0 * r0 + r1 * r1 + r2 * r2;
+        r3[0] = r0;
+        r3[1] = r1;
+        r3[2] = r2;
     }
+    if (a.cs_blocks) block_restrict(a, i < a.nV, i, r3);
     // the tolerance is relative to |b| on the free DOFs (= |r0| when starting from zero)
     const double v[2] = {rr, bb};
     if (block_partials<2>(a, v)) {
@@ -314,23 +318,25 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_spmv(PCGArgs a, int k) {
 __global__ void __launch_bounds__(PCG_THREADS) k_pcg_update(PCGArgs a) {
     if (*(volatile int*)&a.flag[0]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= a.nV) return;
-    const double alpha = a.sc[SC_ALPHA], beta = a.sc[SC_BETA];
-    double r3[3];
+    double r3[3] = {0.0, 0.0, 0.0};
+    if (i < a.nV) {
+        const double alpha = a.sc[SC_ALPHA], beta = a.sc[SC_BETA];
 #pragma unroll
-    for (int d = 0; d < 3; ++d) {
-        const int q = 3 * i + d;
-        const double p = a.u[4 * i + d] + beta * a.p[q];
-        const double s = a.w[q] + beta * a.s[q];
-        a.p[q] = p;
-        a.s[q] = s;
-        a.x[q] += alpha * p;
-        r3[d] = a.r[q] - alpha * s;
-        a.r[q] = r3[d];
+        for (int d = 0; d < 3; ++d) {
+            const int q = 3 * i + d;
+            const double p = a.u[4 * i + d] + beta * a.p[q];
+            const double s = a.w[q] + beta * a.s[q];
+            a.p[q] = p;
+            a.s[q] = s;
+            a.x[q] += alpha * p;
+            r3[d] = a.r[q] - alpha * s;
+            a.r[q] = r3[d];
+        }
+        const double* Mi = a.minv + 9 * (size_t)i;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) a.u[4 * i + d] = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
     }
-    const double* Mi = a.minv + 9 * (size_t)i;
-#pragma unroll
-    for (int d = 0; d < 3; ++d) a.u[4 * i + d] = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
+    if (a.cs_blocks) block_restrict(a, i < a.nV, i, r3);
 }
 
 // ---------------------------------------------------------------- host side
@@ -351,9 +357,15 @@ int launch_elasticity(int nT, const int* tets, const double* x, const double* dm
 int launch_barrier_rows(int type, int n, const int* rows, const double* x, const double* x0, double dh2, double kappa,
                         const double* kap_s, const int* vscene, double* E, double* g, double* Hb, int* status, cudaStream_t s);
 
+int cs_offsets(fipc_ctx* c, const double* x, cudaStream_t s);
+int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t s);
+void cs_apply(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s);
+
 // compute_hessian_and_gradient (NEWTON_IPC.py:736-747) for the current constraint lists
 int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t s) {
-    int st = launch_elasticity(c->nT, c->tets, x, c->dminv, c->vol, c->lam, c->mu, c->dt, nullptr, c->elem_g, c->elem_H, s);
+    int st = cs_offsets(c, x, s);
+    if (st) return st;
+    st = launch_elasticity(c->nT, c->tets, x, c->dminv, c->vol, c->lam, c->mu, c->dt, nullptr, c->elem_g, c->elem_H, s);
     if (st) return st;
     k_assemble_elastic<<<nblk(c->n_upper, 128), 128, 0, s>>>(c->n_upper, c->up_cptr, c->up_contrib, c->up_spos, c->up_tspos,
                                                              c->up_row, c->elem_H, c->mass, c->sell_val);
@@ -472,6 +484,8 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     a.sc = a.part + 3 * nb;
     a.flag = (int*)(c->scal.as<char>() + 48);
     FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 3 * sizeof(int), s));
+    int st = cs_prepare(c, fixed, a, s);
+    if (st) return st;
     // traffic model per launch: matrix blocks and column ids once (padding slots included),
     // row data, the gathered vector once, w written, r read
     const double slots = 32.0 * (double)c->n_slots, nv = (double)c->nV, cn = (double)c->c_nnzb;
@@ -481,6 +495,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     const double upd_flops = nv * 36.0;
     k_pcg_start<<<nb, PCG_THREADS, 0, s>>>(a, c->rhs, rtol);
     FIPC_LAUNCHED();
+    if (a.cs_blocks) cs_apply(c, a, s);
     int h_flag[2] = {0, 0};
     const int chunk = 64;
     for (int k0 = 0; k0 < maxit; k0 += chunk) {
@@ -495,6 +510,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
                 k_pcg_update<<<nb, PCG_THREADS, 0, s>>>(a);
             }
             FIPC_LAUNCHED();
+            if (a.cs_blocks) cs_apply(c, a, s);
         }
         FIPC_CUDA(cudaMemcpyAsync(h_flag, a.flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
         FIPC_CUDA(cudaStreamSynchronize(s));

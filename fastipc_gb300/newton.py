@@ -48,7 +48,7 @@ class Timer:
 
 class NewtonIPC:
     def __init__(self, scene, device='cuda:0', pcg_rtol=1e-10, pcg_maxit=200000, eta=0.2, inversion_filter=True,
-                 max_newton=500, max_halvings=64, pcg_warm_start=False):
+                 max_newton=500, max_halvings=64, pcg_warm_start=False, coarse_agg=None):
         self.scene = scene
         self.device = torch.device(device)
         torch.cuda.set_device(self.device)
@@ -79,6 +79,8 @@ class NewtonIPC:
         kap, idx, nnzb = D(), D(), ctypes.c_int()
         check(L.fipc_ctx_params(ctx, ctypes.byref(kap), ctypes.byref(idx), ctypes.byref(nnzb)), 'fipc_ctx_params')
         self.kappa, self.inv_dx, self.nnzb = kap.value, idx.value, nnzb.value
+        if coarse_agg is not None:
+            self.set_preconditioner(coarse_agg)
         dev = self.device
         self.x = torch.tensor(scene.initial_positions(), dtype=F64, device=dev).contiguous()
         self.v = torch.tensor(scene.v, dtype=F64, device=dev).contiguous()
@@ -125,6 +127,16 @@ class NewtonIPC:
         self.kappa = self.kappa if kappa is None else float(kappa)
         self.inv_dx = self.inv_dx if inv_dx is None else float(inv_dx)
         check(N.lib().fipc_ctx_set_params(self.ctx, D(self.kappa), D(self.inv_dx)), 'fipc_ctx_set_params')
+
+    def set_preconditioner(self, agg_rows):
+        """0: block-Jacobi PCG; a multiple of 128: add the rigid-body coarse space of every run of
+        agg_rows consecutive vertices (the default at creation)."""
+        check(N.lib().fipc_ctx_set_preconditioner(self.ctx, int(agg_rows)), 'fipc_ctx_set_preconditioner')
+
+    def preconditioner(self):
+        a, n = ctypes.c_int(), ctypes.c_int()
+        check(N.lib().fipc_ctx_preconditioner(self.ctx, ctypes.byref(a), ctypes.byref(n)), 'fipc_ctx_preconditioner')
+        return {'agg_rows': a.value, 'coarse_dofs': n.value}
 
     def mass(self):
         m = np.zeros(self.nV)

@@ -70,6 +70,12 @@ int fipc_ctx_params(fipc_ctx* ctx, double* kappa_h, double* inv_dx_h, int* nnzb_
 int fipc_ctx_set_params(fipc_ctx* ctx, double kappa, double inv_dx);
 int fipc_ctx_mass(fipc_ctx* ctx, double* mass_h);
 int fipc_ctx_set_x0(fipc_ctx* ctx, const double* x0, void* stream);
+/* Preconditioner of fipc_solve_system: agg_rows = 0 selects block-Jacobi; a positive multiple of
+ * 128 adds the coarse correction on the six rigid-body modes of every run of agg_rows
+ * consecutive vertices (at most 1024 runs).  The default at creation is 2048 (or larger, so
+ * that there are at most 512 runs).  The solution satisfies the same tolerance either way. */
+int fipc_ctx_set_preconditioner(fipc_ctx* ctx, int agg_rows);
+int fipc_ctx_preconditioner(fipc_ctx* ctx, int* agg_rows, int* n_coarse);
 
 /* find_constraints, NEWTON_IPC.py:337-357 (spatial hash :213-334, dedup :348-356): the seven
  * lists, sorted lexicographically and de-duplicated; counts_h [7] receives their sizes. */
