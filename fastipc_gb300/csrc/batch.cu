@@ -355,21 +355,33 @@ __global__ void __launch_bounds__(TR) k_bpcg_update(BPCG a) {
         const int i = a.tile_row0[t] + threadIdx.x;
         if (i >= a.voff[s + 1]) continue;
         const double alpha = a.sc[SC_COUNT * s + SC_ALPHA], beta = a.sc[SC_COUNT * s + SC_BETA];
+        // every load before the first store (the arrays are not declared distinct)
+        double u[3], p[3], w[3], sv[3], x[3], r[3], M[9];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int q = 3 * i + d;
+            u[d] = a.m.u[4 * i + d];
+            p[d] = a.m.p[q];
+            w[d] = a.m.w[q];
+            sv[d] = a.m.s[q];
+            x[d] = a.m.x[q];
+            r[d] = a.m.r[q];
+        }
+#pragma unroll
+        for (int k = 0; k < 9; ++k) M[k] = __ldg(a.m.minv + 9 * (size_t)i + k);
         double r3[3];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const int q = 3 * i + d;
-            const double p = a.m.u[4 * i + d] + beta * a.m.p[q];
-            const double sv = a.m.w[q] + beta * a.m.s[q];
-            a.m.p[q] = p;
-            a.m.s[q] = sv;
-            a.m.x[q] += alpha * p;
-            r3[d] = a.m.r[q] - alpha * sv;
+            const double pn = u[d] + beta * p[d], sn = w[d] + beta * sv[d];
+            r3[d] = r[d] - alpha * sn;
+            a.m.p[q] = pn;
+            a.m.s[q] = sn;
+            a.m.x[q] = x[d] + alpha * pn;
             a.m.r[q] = r3[d];
         }
-        const double* Mi = a.m.minv + 9 * (size_t)i;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) a.m.u[4 * i + d] = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
+        for (int d = 0; d < 3; ++d) a.m.u[4 * i + d] = M[3 * d] * r3[0] + M[3 * d + 1] * r3[1] + M[3 * d + 2] * r3[2];
     }
 }
 

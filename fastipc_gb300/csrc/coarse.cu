@@ -83,18 +83,19 @@ __device__ __forceinline__ void add_coarse_block(double (&C)[36], const double* 
 
 // one CTA per coupled aggregate pair (I, J): the 6x6 block Ac[I][J] = sum over free i in I and
 // free j in J of P_i^T A_ij P_j (elastic + inertia blocks), fixed-order sums, into dense Ac
-__global__ void __launch_bounds__(CS_THREADS) k_cs_build(int nV, int agg_rows, int n, const int* __restrict__ pairs,
+constexpr int CS_BUILD_THREADS = 512;
+__global__ void __launch_bounds__(CS_BUILD_THREADS) k_cs_build(int nV, int agg_rows, int n, const int* __restrict__ pairs,
                                                          const int* __restrict__ soff, const int* __restrict__ scol,
                                                          const int* __restrict__ rlen, const double* __restrict__ sval,
                                                          const unsigned char* __restrict__ fixed, const double* __restrict__ d,
                                                          double* __restrict__ Ac) {
-    __shared__ double sh[36][CS_THREADS / 32];
+    __shared__ double sh[36][CS_BUILD_THREADS / 32];
     const int I = pairs[2 * blockIdx.x], J = pairs[2 * blockIdx.x + 1];
     const int i0 = I * agg_rows, i1 = min(nV, i0 + agg_rows), j0 = J * agg_rows, j1 = min(nV, j0 + agg_rows);
     double C[36];
 #pragma unroll
     for (int e = 0; e < 36; ++e) C[e] = 0.0;
-    for (int i = i0 + threadIdx.x; i < i1; i += CS_THREADS) {
+    for (int i = i0 + threadIdx.x; i < i1; i += CS_BUILD_THREADS) {
         if (fixed[i]) continue;
         const double di[3] = {d[3 * (size_t)i], d[3 * (size_t)i + 1], d[3 * (size_t)i + 2]};
         const int sl = i >> 5, lane = i & 31, base = soff[sl], len = rlen[i];
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(CS_THREADS) k_cs_build(int nV, int agg_rows, i
     __syncthreads();
     if (threadIdx.x < 36) {
         double t = 0.0;
-        for (int w = 0; w < CS_THREADS / 32; ++w) t += sh[threadIdx.x][w];
+        for (int w = 0; w < CS_BUILD_THREADS / 32; ++w) t += sh[threadIdx.x][w];
         const int r = threadIdx.x / 6, c = threadIdx.x % 6;
         Ac[(size_t)(6 * I + r) * n + 6 * J + c] = t;
     }
@@ -166,38 +167,25 @@ __global__ void k_cs_gauss_jordan(int n, double* __restrict__ A, double* __restr
     }
 }
 
-// y = Ac^-1 g with g_I = sum of the restriction partials of aggregate I's PCG blocks (fixed
-// order); every CTA forms g in shared memory, then one warp per row
-constexpr int CS_MV_THREADS = 256;
-__global__ void __launch_bounds__(CS_MV_THREADS) k_cs_coarse(PCGArgs a, int n, int nb, const double* __restrict__ Ainv) {
-    extern __shared__ double g[];
+// u_i += P_i y_I = y_t + y_w x d_i on free vertices, y_I = rows 6I..6I+5 of Ac^-1 times g: each
+// block (one aggregate) forms its own six values, so the correction is one launch
+__global__ void __launch_bounds__(PCG_THREADS) k_cs_prolong(PCGArgs a) {
+    __shared__ double y[6];
     if (*(volatile int*)&a.flag[0]) return;
-    for (int q = threadIdx.x; q < n; q += CS_MV_THREADS) {
-        const int I = q / 6, c = q % 6;
-        const int b0 = I * a.cs_blocks, b1 = min(nb, b0 + a.cs_blocks);
+    const int I = blockIdx.x / a.cs_blocks;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int k = wid; k < 6; k += PCG_THREADS / 32) {
+        const double* Ar = a.cs_ainv + (size_t)(6 * I + k) * a.cs_n;
         double t = 0.0;
-        for (int b = b0; b < b1; ++b) t += a.cs_part[6 * (size_t)b + c];
-        g[q] = t;
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warps = CS_MV_THREADS / 32;
-    for (int row = blockIdx.x * warps + (threadIdx.x >> 5); row < n; row += gridDim.x * warps) {
-        const double* Ar = Ainv + (size_t)row * n;
-        double t = 0.0;
-        for (int j = lane; j < n; j += 32) t += Ar[j] * g[j];
+        for (int j = lane; j < a.cs_n; j += 32) t += __ldg(Ar + j) * __ldg(a.cs_g + j);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if (lane == 0) a.cs_y[row] = t;
+        if (lane == 0) y[k] = t;
     }
-}
-
-// u_i += P_i y_I = y_t + y_w x d_i on free vertices
-__global__ void __launch_bounds__(PCG_THREADS) k_cs_prolong(PCGArgs a, int agg_rows) {
-    if (*(volatile int*)&a.flag[0]) return;
+    __syncthreads();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nV || a.fixed[i]) return;
-    const double* y = a.cs_y + 6 * (size_t)(i / agg_rows);
-    const double dx = a.cs_d[3 * (size_t)i], dy = a.cs_d[3 * (size_t)i + 1], dz = a.cs_d[3 * (size_t)i + 2];
+    const double dx = __ldg(a.cs_d + 3 * (size_t)i), dy = __ldg(a.cs_d + 3 * (size_t)i + 1), dz = __ldg(a.cs_d + 3 * (size_t)i + 2);
     a.u[4 * (size_t)i] += y[0] + (y[4] * dz - y[5] * dy);
     a.u[4 * (size_t)i + 1] += y[1] + (y[5] * dx - y[3] * dz);
     a.u[4 * (size_t)i + 2] += y[2] + (y[3] * dy - y[4] * dx);
@@ -250,11 +238,13 @@ int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
     a.cs_blocks = 0;
     if (!c->cs_agg_rows) return FIPC_OK;
     const int n = 6 * c->cs_n_agg, nb = nblk_c(c->nV, PCG_THREADS);
-    if (c->cs_Ac.ensure(8ll * n * n) || c->cs_buf.ensure(8ll * 4 * n) || c->cs_part.ensure(48ll * nb) || c->cs_y.ensure(8ll * n))
+    if (c->cs_Ac.ensure(8ll * n * n) || c->cs_buf.ensure(8ll * 4 * n) || c->cs_part.ensure(48ll * nb) || c->cs_gbuf.ensure(8ll * n) ||
+        c->cs_tick.ensure(4ll * c->cs_n_agg))
         return FIPC_ERR_CUDA;
+    FIPC_CUDA(cudaMemsetAsync(c->cs_tick.p, 0, 4ll * c->cs_n_agg, s));   // aggregate tickets
     double* Ac = c->cs_Ac.as<double>();
     FIPC_CUDA(cudaMemsetAsync(Ac, 0, 8ll * n * n, s));
-    k_cs_build<<<c->cs_n_pairs, CS_THREADS, 0, s>>>(c->nV, c->cs_agg_rows, n, c->cs_pairs, c->sell_off, c->sell_col, c->row_len,
+    k_cs_build<<<c->cs_n_pairs, CS_BUILD_THREADS, 0, s>>>(c->nV, c->cs_agg_rows, n, c->cs_pairs, c->sell_off, c->sell_col, c->row_len,
                                                     c->sell_val, fixed, c->cs_d.as<double>(), Ac);
     FIPC_LAUNCHED();
     k_cs_regularize<<<nblk_c(n, 128), 128, 0, s>>>(n, Ac);
@@ -275,25 +265,24 @@ int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
     a.cs_blocks = c->cs_agg_rows / PCG_THREADS;
     a.cs_d = c->cs_d.as<double>();
     a.cs_part = c->cs_part.as<double>();
-    a.cs_y = c->cs_y.as<double>();
+    a.cs_g = c->cs_gbuf.as<double>();
+    a.cs_ticket = c->cs_tick.as<int>();
+    a.cs_ainv = Ac;
+    a.cs_n = n;
     FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
 }
 
-// the coarse correction u += P Ac^-1 P^T r for the restriction partials the last PCG kernel wrote
+// the coarse correction u += P Ac^-1 P^T r for the aggregate restrictions the last PCG kernel wrote
 void cs_apply(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s) {
-    const int n = 6 * c->cs_n_agg, nb = nblk_c(c->nV, PCG_THREADS);
-    const int grid = nblk_c(n, CS_MV_THREADS / 32);
-    k_cs_coarse<<<grid, CS_MV_THREADS, 8 * n, s>>>(a, n, nb, c->cs_Ac.as<double>());
-    FIPC_LAUNCHED();
-    k_cs_prolong<<<nb, PCG_THREADS, 0, s>>>(a, c->cs_agg_rows);
+    k_cs_prolong<<<nblk_c(c->nV, PCG_THREADS), PCG_THREADS, 0, s>>>(a);
     FIPC_LAUNCHED();
 }
 
 void cs_free(fipc_ctx* c) {
     if (c->cs_pairs) cudaFree(c->cs_pairs);
     c->cs_pairs = nullptr;
-    DBuf* bufs[] = {&c->cs_d, &c->cs_Ac, &c->cs_diag, &c->cs_buf, &c->cs_part, &c->cs_y};
+    DBuf* bufs[] = {&c->cs_d, &c->cs_Ac, &c->cs_tick, &c->cs_buf, &c->cs_part, &c->cs_gbuf};
     for (DBuf* b : bufs) b->release();
 }
 

@@ -94,7 +94,7 @@ struct fipc_ctx_impl {
     // each aggregate of cs_agg_rows consecutive vertices (0: block-Jacobi only)
     int cs_agg_rows = 0, cs_n_agg = 0, cs_n_pairs = 0;
     int* cs_pairs = nullptr;              // [cs_n_pairs][2] aggregate pairs coupled by the pattern
-    DBuf cs_d, cs_Ac, cs_diag, cs_buf, cs_part, cs_y;
+    DBuf cs_d, cs_Ac, cs_tick, cs_buf, cs_part, cs_gbuf;
     // grids
     Grid gp, ge;
     // small device scalars: [0] alpha bits, [1] hit flag, reductions ...

@@ -297,19 +297,23 @@ __global__ void k_row_dist(int type, int n, const int4* __restrict__ rows, const
     for (int k = 0; k < nv; ++k) atomicMin(dmin + id[k], bits);
 }
 
-// X[i] = (16 one-ring relative positions / h, v dt / h, dx_prev / h, min(dist / dhat, 1), 0 pad)
+// X[i] = (16 one-ring relative positions / h, v dt / h, dx_prev / h, min(dist / dhat, 1), 0 pad);
+// relative positions are x_j - x_i, or (x_j - x_i) - (X_j - X_i) against the rest shape X when
+// x0 is given (the one-ring's deformation)
 __global__ void k_features(int nV, const int* __restrict__ rp, const int* __restrict__ ci, const double* __restrict__ x,
-                           const double* __restrict__ v, const double* __restrict__ dxp, double dt, double inv_h, double inv_dhat,
-                           const unsigned* __restrict__ dmin, float* __restrict__ X) {
+                           const double* __restrict__ x0, const double* __restrict__ v, const double* __restrict__ dxp, double dt,
+                           double inv_h, double inv_dhat, const unsigned* __restrict__ dmin, float* __restrict__ X) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nV) return;
     float* f = X + (size_t)i * MLP_IN;
     const v3 xi = ld3(x, i);
+    const v3 Xi = x0 ? ld3(x0, i) : mk(0, 0, 0);
     int k = 0;
     for (int e = rp[i]; e < rp[i + 1] && k < MLP_NBR; ++e) {
         const int j = ci[e];
         if (j == i) continue;
-        const v3 d = ld3(x, j) - xi;
+        v3 d = ld3(x, j) - xi;
+        if (x0) d = d - (ld3(x0, j) - Xi);
         f[3 * k] = (float)(d.x * inv_h);
         f[3 * k + 1] = (float)(d.y * inv_h);
         f[3 * k + 2] = (float)(d.z * inv_h);
@@ -330,8 +334,8 @@ __global__ void k_features(int nV, const int* __restrict__ rp, const int* __rest
 
 }  // namespace fipc
 
-extern "C" int fipc_mlp_features(fipc_ctx* c, const double* x, const double* v, const double* dx_prev, double h, float* X,
-                                 void* stream) {
+extern "C" int fipc_mlp_features(fipc_ctx* c, const double* x, const double* v, const double* dx_prev, double h, int rest_relative,
+                                 float* X, void* stream) {
     if (!c || !x || !v || !dx_prev || !X || !(h > 0)) return FIPC_ERR_ARGUMENT;
     cudaStream_t s = (cudaStream_t)stream;
     if (c->mlp_dist.ensure(4ll * c->nV)) return FIPC_ERR_CUDA;
@@ -343,8 +347,50 @@ extern "C" int fipc_mlp_features(fipc_ctx* c, const double* x, const double* v, 
         k_row_dist<<<nblk(c->h_counts[t], 128), 128, 0, s>>>(t, c->h_counts[t], c->rows[t].as<int4>(), x, dmin);
         FIPC_LAUNCHED();
     }
-    k_features<<<nblk(c->nV, 128), 128, 0, s>>>(c->nV, c->row_ptr, c->col_idx, x, v, dx_prev, c->dt, 1.0 / h, 1.0 / c->dhat, dmin, X);
+    k_features<<<nblk(c->nV, 128), 128, 0, s>>>(c->nV, c->row_ptr, c->col_idx, x, rest_relative ? c->x0 : nullptr, v, dx_prev, c->dt,
+                                                1.0 / h, 1.0 / c->dhat, dmin, X);
     FIPC_LAUNCHED();
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+
+// ---------------------------------------------------------------- smoothing of a displacement
+namespace fipc {
+// out_i = mean of d_j over the one-ring of i including i (the elastic block pattern); 0 on
+// Dirichlet vertices
+__global__ void k_ring_mean(int nV, const int* __restrict__ rp, const int* __restrict__ ci, const unsigned char* __restrict__ fixed,
+                            const double* __restrict__ d, double* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV) return;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    if (!fixed[i]) {
+        for (int e = rp[i]; e < rp[i + 1]; ++e) {
+            const int j = ci[e];
+            s0 += d[3 * (size_t)j];
+            s1 += d[3 * (size_t)j + 1];
+            s2 += d[3 * (size_t)j + 2];
+        }
+        const double inv = 1.0 / (double)(rp[i + 1] - rp[i]);
+        s0 *= inv;
+        s1 *= inv;
+        s2 *= inv;
+    }
+    out[3 * (size_t)i] = s0;
+    out[3 * (size_t)i + 1] = s1;
+    out[3 * (size_t)i + 2] = s2;
+}
+}  // namespace fipc
+
+// passes of one-ring averaging of d [V][3] (in place, tmp: scratch [V][3]); the learned
+// correction is smoothed so that its vertex-to-vertex noise does not load the elastic energy
+extern "C" int fipc_mlp_smooth(fipc_ctx* c, const unsigned char* fixed, double* d, double* tmp, int passes, void* stream) {
+    if (!c || !fixed || !d || !tmp || passes < 0) return FIPC_ERR_ARGUMENT;
+    cudaStream_t s = (cudaStream_t)stream;
+    for (int k = 0; k < passes; ++k) {
+        k_ring_mean<<<nblk(c->nV, 128), 128, 0, s>>>(c->nV, c->row_ptr, c->col_idx, fixed, d, tmp);
+        FIPC_LAUNCHED();
+        FIPC_CUDA(cudaMemcpyAsync(d, tmp, 24ll * c->nV, cudaMemcpyDeviceToDevice, s));
+    }
     FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
 }

@@ -22,7 +22,10 @@ struct PCGArgs {
     int cs_blocks;
     const double* cs_d;              // [V][3] vertex offset from its aggregate's centroid
     double* cs_part;                 // [nblk][6] per-block restriction (force, torque) of r
-    double* cs_y;                    // [6 n_agg] coarse correction
+    double* cs_g;                    // [6 n_agg] restriction per aggregate
+    int* cs_ticket;                  // [n_agg] blocks of the aggregate done (reset by its last block)
+    const double* cs_ainv;           // [6 n_agg]^2 inverse coarse matrix
+    int cs_n;                        // 6 n_agg
 };
 enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
 constexpr int PCG_THREADS = 128;
@@ -93,19 +96,21 @@ __device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double*
     }
 }
 
-// restriction of one block's residuals onto the rigid-body modes of its aggregate:
-// sum over rows of (r_i, d_i x r_i) into cs_part[block] (fixed shuffle / shared order)
-__device__ __forceinline__ void block_restrict(const PCGArgs& a, bool valid, int i, const double (&r)[3]) {
+// restriction of one block's residuals onto the rigid-body modes of its aggregate: the block's
+// sum over rows of (r_i, d_i x r_i) into cs_part[block] (fixed shuffle / shared order); the
+// aggregate's last block to finish (atomic ticket) sums its blocks' partials in block order
+// into cs_g, so the aggregate totals need no extra launch and are reproducible
+__device__ __forceinline__ void block_restrict(const PCGArgs& a, bool valid, int i, const double (&r)[3], const double (&d)[3]) {
     __shared__ double sh[6][PCG_THREADS / 32];
+    __shared__ bool last;
     double v[6] = {0, 0, 0, 0, 0, 0};
     if (valid) {
-        const double dx = a.cs_d[3 * (size_t)i], dy = a.cs_d[3 * (size_t)i + 1], dz = a.cs_d[3 * (size_t)i + 2];
         v[0] = r[0];
         v[1] = r[1];
         v[2] = r[2];
-        v[3] = dy * r[2] - dz * r[1];
-        v[4] = dz * r[0] - dx * r[2];
-        v[5] = dx * r[1] - dy * r[0];
+        v[3] = d[1] * r[2] - d[2] * r[1];
+        v[4] = d[2] * r[0] - d[0] * r[2];
+        v[5] = d[0] * r[1] - d[1] * r[0];
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -116,10 +121,26 @@ __device__ __forceinline__ void block_restrict(const PCGArgs& a, bool valid, int
         if (lane == 0) sh[c][wid] = x;
     }
     __syncthreads();
+    const int I = blockIdx.x / a.cs_blocks;
     if (threadIdx.x < 6) {
         double t = 0.0;
         for (int k = 0; k < PCG_THREADS / 32; ++k) t += sh[threadIdx.x][k];
         a.cs_part[6 * (size_t)blockIdx.x + threadIdx.x] = t;
+        __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nblocks = min((int)gridDim.x - I * a.cs_blocks, a.cs_blocks);
+        last = atomicAdd(&a.cs_ticket[I], 1) == nblocks - 1;
+    }
+    __syncthreads();
+    if (last && threadIdx.x < 6) {
+        __threadfence();
+        const int b0 = I * a.cs_blocks, b1 = min((int)gridDim.x, b0 + a.cs_blocks);
+        double t = 0.0;
+        for (int b = b0; b < b1; ++b) t += *(volatile double*)&a.cs_part[6 * (size_t)b + threadIdx.x];
+        a.cs_g[6 * I + threadIdx.x] = t;
+        if (threadIdx.x == 0) a.cs_ticket[I] = 0;
     }
 }
 

@@ -257,7 +257,12 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const doub
         r3[1] = r1;
         r3[2] = r2;
     }
-    if (a.cs_blocks) block_restrict(a, i < a.nV, i, r3);
+    if (a.cs_blocks) {
+        double d3[3] = {0.0, 0.0, 0.0};
+        if (i < a.nV)
+            for (int k = 0; k < 3; ++k) d3[k] = a.cs_d[3 * (size_t)i + k];
+        block_restrict(a, i < a.nV, i, r3, d3);
+    }
     // the tolerance is relative to |b| on the free DOFs (= |r0| when starting from zero)
     const double v[2] = {rr, bb};
     if (block_partials<2>(a, v)) {
@@ -318,25 +323,45 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_spmv(PCGArgs a, int k) {
 __global__ void __launch_bounds__(PCG_THREADS) k_pcg_update(PCGArgs a) {
     if (*(volatile int*)&a.flag[0]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    double r3[3] = {0.0, 0.0, 0.0};
+    double rn[3] = {0.0, 0.0, 0.0}, d3[3] = {0.0, 0.0, 0.0};
     if (i < a.nV) {
         const double alpha = a.sc[SC_ALPHA], beta = a.sc[SC_BETA];
+        // every load before the first store: the vectors are separate arrays, but nothing tells
+        // the compiler so, and a store between two loads would serialise them
+        double u[3], p[3], w[3], s[3], x[3], r[3], M[9];
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
             const int q = 3 * i + d;
-            const double p = a.u[4 * i + d] + beta * a.p[q];
-            const double s = a.w[q] + beta * a.s[q];
-            a.p[q] = p;
-            a.s[q] = s;
-            a.x[q] += alpha * p;
-            r3[d] = a.r[q] - alpha * s;
-            a.r[q] = r3[d];
+            u[d] = a.u[4 * i + d];
+            p[d] = a.p[q];
+            w[d] = a.w[q];
+            s[d] = a.s[q];
+            x[d] = a.x[q];
+            r[d] = a.r[q];
         }
-        const double* Mi = a.minv + 9 * (size_t)i;
 #pragma unroll
-        for (int d = 0; d < 3; ++d) a.u[4 * i + d] = Mi[3 * d] * r3[0] + Mi[3 * d + 1] * r3[1] + Mi[3 * d + 2] * r3[2];
+        for (int k = 0; k < 9; ++k) M[k] = __ldg(a.minv + 9 * (size_t)i + k);
+        if (a.cs_blocks)
+#pragma unroll
+            for (int d = 0; d < 3; ++d) d3[d] = __ldg(a.cs_d + 3 * (size_t)i + d);
+        double pn[3], sn[3];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            pn[d] = u[d] + beta * p[d];
+            sn[d] = w[d] + beta * s[d];
+            rn[d] = r[d] - alpha * sn[d];
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const int q = 3 * i + d;
+            a.p[q] = pn[d];
+            a.s[q] = sn[d];
+            a.x[q] = x[d] + alpha * pn[d];
+            a.r[q] = rn[d];
+            a.u[4 * i + d] = M[3 * d] * rn[0] + M[3 * d + 1] * rn[1] + M[3 * d + 2] * rn[2];
+        }
     }
-    if (a.cs_blocks) block_restrict(a, i < a.nV, i, r3);
+    if (a.cs_blocks) block_restrict(a, i < a.nV, i, rn, d3);
 }
 
 // ---------------------------------------------------------------- host side

@@ -108,13 +108,15 @@ def _init_params(seed):
     return np.concatenate([a.ravel() for a in parts]).astype(np.float32)
 
 
-def features(sim, X=None):
-    """Per-vertex inputs at the current state (constraint lists of the last find_constraints)."""
+def features(sim, X=None, rest_relative=True):
+    """Per-vertex inputs at the current state (constraint lists of the last find_constraints);
+    one-ring positions relative to the rest shape's (the local deformation) by default."""
     if X is None:
         X = torch.empty((sim.nV, WarmStartMLP.IN), dtype=F32, device=sim.device)
     h = 1.0 / sim.inv_dx
     check(N.lib().fipc_mlp_features(sim.ctx, N.dptr(sim.x, torch.float64), N.dptr(sim.v, torch.float64),
-                                    N.dptr(sim.dx_prev, torch.float64), ctypes.c_double(h), _p(X), N.stream()), 'mlp_features')
+                                    N.dptr(sim.dx_prev, torch.float64), ctypes.c_double(h), int(rest_relative), _p(X),
+                                    N.stream()), 'mlp_features')
     return X
 
 
@@ -126,10 +128,11 @@ class LearnedStart:
     lengths of the chosen candidates.
     """
 
-    def __init__(self, model=None, kind='mlp'):
+    def __init__(self, model=None, kind='mlp', smooth=4):
         assert kind in ('mlp', 'inertial')
         assert kind == 'inertial' or model is not None
-        self.model, self.kind = model, kind
+        self.model, self.kind, self.smooth = model, kind, smooth
+        self._tmp = None
         self.chosen = {'plain': 0, 'inertial': 0, 'mlp': 0}
         self.alphas = []
         self._X = None
@@ -147,13 +150,19 @@ class LearnedStart:
         return torch.where(free, sim.xTilde - sim.x, torch.zeros_like(sim.x))
 
     def learned(self, sim, d0):
-        """d0 + s h out; needs the constraint lists of the current positions (features)."""
+        """d0 + S(s h out), S = ``smooth`` passes of one-ring averaging; needs the constraint
+        lists of the current positions (features)."""
         if self._X is None or self._X.shape[0] != sim.nV:
             self._X = torch.empty((sim.nV, WarmStartMLP.IN), dtype=F32, device=sim.device)
+            self._tmp = torch.empty((sim.nV, 3), dtype=torch.float64, device=sim.device)
         X = features(sim, self._X)
         out = self.model.forward(X)
-        d = d0 + out[:, :3].to(torch.float64) * (self.model.scale / sim.inv_dx)
-        return torch.where((sim.fixed == 0).unsqueeze(1), d, torch.zeros_like(d))
+        corr = torch.where((sim.fixed == 0).unsqueeze(1), out[:, :3].to(torch.float64) * (self.model.scale / sim.inv_dx),
+                           torch.zeros_like(d0)).contiguous()
+        if self.smooth:
+            check(N.lib().fipc_mlp_smooth(sim.ctx, N.dptr(sim.fixed, torch.uint8), N.dptr(corr, torch.float64),
+                                          N.dptr(self._tmp, torch.float64), int(self.smooth), N.stream()), 'mlp_smooth')
+        return d0 + corr
 
     def _filtered(self, sim, d):
         """x = x^n + alpha d with alpha from the CCD filter and collision halving; its energy."""
@@ -381,12 +390,14 @@ def experiment_bar(out_dir, nx=400, train_steps=30, eval_steps=30, device='cuda:
     model.save(os.path.join(out_dir, f'warmstart_bar{nx}.npz'))
     snap = (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone())
     xs = {}
-    for mode in ('plain', 'inertial', 'mlp'):
+    modes = {'plain': None, 'inertial': ('inertial', 0), 'mlp': ('mlp', 0), 'mlp_s2': ('mlp', 2), 'mlp_s4': ('mlp', 4),
+             'mlp_s8': ('mlp', 8)}
+    for mode, spec in modes.items():
         sim.x.copy_(snap[0])
         sim.v.copy_(snap[1])
         sim.dx_prev.copy_(snap[2])
         sim.newton_iters, sim.pcg_iters = [], []
-        guess = None if mode == 'plain' else LearnedStart(model if mode == 'mlp' else None, kind=mode)
+        guess = None if spec is None else LearnedStart(model if spec[0] == 'mlp' else None, kind=spec[0], smooth=spec[1])
         sim.initial_guess = guess
         inter = 0
         torch.cuda.synchronize()
@@ -398,8 +409,9 @@ def experiment_bar(out_dir, nx=400, train_steps=30, eval_steps=30, device='cuda:
         res[mode] = _result(sim, guess, eval_steps, time.perf_counter() - t1, inter)
         xs[mode] = sim.x.cpu().numpy()
         log(f"bar {mode}: newton {res[mode]['newton']} pcg {res[mode]['pcg']} wall {res[mode]['wall_s']:.2f} s")
-    for mode in ('inertial', 'mlp'):
-        res[mode]['max_dev_vs_plain'] = float(np.abs(xs[mode] - xs['plain']).max())
+    for mode in modes:
+        if mode != 'plain':
+            res[mode]['max_dev_vs_plain'] = float(np.abs(xs[mode] - xs['plain']).max())
     sim.close()
     with open(os.path.join(out_dir, f'warmstart_bar{nx}.json'), 'w') as fh:
         json.dump(res, fh, indent=1)

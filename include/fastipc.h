@@ -140,11 +140,15 @@ int fipc_mlp_mse(int n, const float* out, const float* target, float* dout, floa
 /* one Adam step, t >= 1 */
 int fipc_mlp_adam(int n_params, float* params, const float* grads, float* m, float* v, float lr, float beta1, float beta2,
                   float eps, int t, void* stream);
-/* per-vertex inputs X [V][64] at positions x: 16 one-ring relative positions / h, v dt / h,
- * dx_prev / h (the Python driver passes the displacement of the step before the last one),
- * min(nearest constraint distance / d-hat, 1) over the lists of the last fipc_find_constraints */
-int fipc_mlp_features(fipc_ctx* ctx, const double* x, const double* v, const double* dx_prev, double h, float* X,
-                      void* stream);
+/* per-vertex inputs X [V][64] at positions x: 16 one-ring relative positions / h (x_j - x_i, or
+ * with rest_relative (x_j - x_i) - (X_j - X_i) against the rest shape), v dt / h, dx_prev / h
+ * (the Python driver passes the displacement of the step before the last one), min(nearest
+ * constraint distance / d-hat, 1) over the lists of the last fipc_find_constraints */
+int fipc_mlp_features(fipc_ctx* ctx, const double* x, const double* v, const double* dx_prev, double h, int rest_relative,
+                      float* X, void* stream);
+/* passes of one-ring averaging of a displacement d [V][3] over the elastic block pattern, zero on
+ * Dirichlet vertices (in place; tmp: scratch [V][3]) */
+int fipc_mlp_smooth(fipc_ctx* ctx, const unsigned char* fixed, double* d, double* tmp, int passes, void* stream);
 
 /* ---- batched scenes ---------------------------------------------------------------------- *
  * S independent scenes (1 <= S <= 1024) in one context, each stepping its own Newton loop of

@@ -16,11 +16,20 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 
-def settled(seed, steps=4):
+def on_ground(sc, s):
+    ground = set(range(len(sc.x) - 8, len(sc.x)))
+    s.find_constraints()
+    return any(int(v) in ground for r in s.constraints() for v in r.ravel())
+
+
+def settled(seed, max_steps=30):
+    """the stack stepped until its lowest cube is within d-hat of the ground box"""
     sc = scenes.cube_stack(seed, max_cubes=3, max_hex=5)
     s = NewtonIPC(sc, pcg_rtol=1e-12)
-    for f in range(steps):
+    for f in range(max_steps):
         s.step(f)
+        if on_ground(sc, s):
+            break
     return sc, s
 
 

@@ -113,10 +113,12 @@ def contact_sim():
     s.close()
 
 
-def test_features_match_numpy(contact_sim):
+@pytest.mark.parametrize('rest_relative', [False, True])
+def test_features_match_numpy(contact_sim, rest_relative):
     s = contact_sim
     assert sum(s.counts) > 0, 'scene should be in contact'
-    X = features(s).cpu().numpy()
+    X = features(s, rest_relative=rest_relative).cpu().numpy()
+    X0 = np.asarray(s.scene.x, np.float64)
     A, _, _ = s.export_system()
     rp, ci = A.indptr, A.indices
     x, v, dxp = s.x.cpu().numpy(), s.v.cpu().numpy(), s.dx_prev.cpu().numpy()
@@ -126,7 +128,10 @@ def test_features_match_numpy(contact_sim):
     for i in range(s.nV):
         nb = [j for j in ci[rp[i]:rp[i + 1]] if j != i][:16]
         for k, j in enumerate(nb):
-            ref[i, 3 * k:3 * k + 3] = ((x[j] - x[i]) * (1.0 / h)).astype(np.float32)
+            d = x[j] - x[i]
+            if rest_relative:
+                d = d - (X0[j] - X0[i])
+            ref[i, 3 * k:3 * k + 3] = (d * (1.0 / h)).astype(np.float32)
     ref[:, 48:51] = (v * s.dt * (1.0 / h)).astype(np.float32)
     ref[:, 51:54] = (dxp * (1.0 / h)).astype(np.float32)
     dmin = np.full(s.nV, np.inf, np.float32)
