@@ -47,6 +47,9 @@ def parse():
     ap.add_argument('--workload', default='bar', choices=['bar', 'batch'],
                     help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context')
     ap.add_argument('--scenes', type=int, default=512, help='scenes of the batch workload')
+    ap.add_argument('--learned-steps', type=int, default=20,
+                    help='steps run from the timed state with the inertial and the learned start (0: skip)')
+    ap.add_argument('--learned-weights', default=os.path.join(HERE, 'fastipc_gb300', 'weights', 'warmstart_bar400.npz'))
     return ap.parse_args()
 
 
@@ -225,7 +228,7 @@ def main():
     for _ in range(args.warmup):
         sim.step(f)
         f += 1
-    snap = (sim.x.clone(), sim.v.clone())
+    snap = (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone())
     hist = {k: v.clone() for k, v in sim._dir_hist.items()}
     f0 = f
     n_newton0, n_pcg0 = len(sim.newton_iters), len(sim.pcg_iters)
@@ -282,6 +285,8 @@ def main():
         e2e_ms = float(t.item())
     nbytes = 2 * sim.x.numel() * 8
 
+    learned = learned_leg(sim, snap, f0, args) if args.learned_steps > 0 else None
+
     if rank == 0:
         pk, src = peaks()
         achieved = pb / (pt / 1e3) / 1e9 if pt > 0 else None
@@ -305,6 +310,8 @@ def main():
                        'd2h_bytes_per_step': nbytes},
                'gpu_launches': launches, 'roofline': roof, 'clocks': clk.summary(),
                'sections_s': {k: round(v, 4) for k, v in sim.timer.total.items()}}
+        if learned:
+            out['learned_warm_start'] = learned
         if world == 1 and not args.no_cpu_baseline:
             out['cpu_baseline'] = cpu_baseline(scene, newton_per_step, pcg_per_newton, args)
         print(json.dumps(out), flush=True)
@@ -429,6 +436,31 @@ def batch_cpu(scs, args, budget_s=20.0):
             break
     sample = f'one time step (step {args.warmup}) of scenes {names} stepped one at a time, {t_total:.1f} s'
     return done / t_total, sample, O.lib().oracle_num_threads()
+
+
+def learned_leg(sim, snap, f0, args):
+    """Newton iterations per step from the timed state with the plain (reference), inertial and
+    learned starts, the same steps each (outside the timed value).  The network was trained on
+    another jitter seed of the same bar."""
+    from fastipc_gb300.learned import LearnedStart, WarmStartMLP, compare_starts
+    if not os.path.exists(args.learned_weights):
+        return {'unavailable': f'no weights at {os.path.relpath(args.learned_weights, HERE)}'}
+    model = WarmStartMLP.load(args.learned_weights, device=sim.device)
+    sim.x.copy_(snap[0])
+    sim.v.copy_(snap[1])
+    sim.dx_prev.copy_(snap[2])
+    warm = sim.pcg_warm_start
+    sim.pcg_warm_start = False
+    modes = {'plain': None, 'inertial': LearnedStart(kind='inertial'), 'learned': LearnedStart(model, kind='mlp', smooth=4)}
+    r = compare_starts(sim, args.learned_steps, f0, modes, log=None)
+    sim.pcg_warm_start = warm
+    out = {'steps': args.learned_steps, 'first_step': f0, 'weights': os.path.relpath(args.learned_weights, HERE)}
+    for k, v in r.items():
+        out[k] = {'newton_iters_per_step': v['newton'] / v['steps'], 'steps_per_s': v['steps'] / v['wall_s'],
+                  'pcg_iters': v['pcg'], 'intersecting_steps': v['intersecting_steps'], 'chosen': v.get('chosen')}
+    out['newton_reduction_vs_inertial'] = 1.0 - r['learned']['newton'] / max(r['inertial']['newton'], 1)
+    out['newton_reduction_vs_plain'] = 1.0 - r['learned']['newton'] / max(r['plain']['newton'], 1)
+    return out
 
 
 def ctypes_read(L):

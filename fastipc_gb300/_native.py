@@ -25,7 +25,7 @@ EXPORTS = [
     'fipc_compute_energy_noalloc', 'fipc_mlp_param_count', 'fipc_mlp_forward', 'fipc_mlp_backward', 'fipc_mlp_mse',
     'fipc_mlp_adam', 'fipc_mlp_features', 'fipc_batch_create', 'fipc_batch_params', 'fipc_batch_compute_energy',
     'fipc_batch_output_residual', 'fipc_batch_step_size', 'fipc_batch_check_collision', 'fipc_batch_apply_sol',
-    'fipc_batch_solve_system', 'fipc_batch_pcg_shape', 'fipc_ctx_set_preconditioner', 'fipc_ctx_preconditioner', 'fipc_mlp_smooth',
+    'fipc_batch_solve_system', 'fipc_batch_pcg_shape', 'fipc_ctx_set_preconditioner', 'fipc_ctx_preconditioner', 'fipc_mlp_smooth', 'fipc_dense_spd_inverse',
 ]
 
 

@@ -113,15 +113,53 @@ __global__ void k_cell_emit(int mode, int n, const int* __restrict__ prim, const
             }
 }
 
-// position of key in the sorted unique keys, or -1
-__device__ __forceinline__ int find_cell(const unsigned long long* __restrict__ uk, int nu, unsigned long long key) {
-    int lo = 0, hi = nu;
-    while (lo < hi) {
-        const int m = (lo + hi) >> 1;
-        if (__ldg(uk + m) < key) lo = m + 1;
-        else hi = m;
+// Cell lookup of a built grid: an open-addressing table (linear probing, load factor <= 1/2)
+// maps each occupied cell key to its run of ids, so a query cell costs one or two probes instead
+// of a binary search over all keys.  The table holds exactly the sorted grid's runs; which slot a
+// key lands in depends on insertion order, the run it maps to does not.
+constexpr unsigned long long HASH_EMPTY = ~0ull;
+__device__ __forceinline__ unsigned long long mix64(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return k;
+}
+struct GridView {
+    const unsigned long long* hk;   // table keys
+    const int* hv;                  // table values: run index
+    unsigned long long mask;        // table size - 1
+    const int* us;                  // run starts
+    const int* ids;                 // primitive ids by run
+    // run index of key, or -1 (at most mask + 1 probes)
+    __device__ __forceinline__ int find(unsigned long long key) const {
+        unsigned long long h = mix64(key) & mask;
+        for (unsigned long long n = 0; n <= mask; ++n) {
+            const unsigned long long k = __ldg(hk + h);
+            if (k == key) return __ldg(hv + h);
+            if (k == HASH_EMPTY) return -1;
+            h = (h + 1) & mask;
+        }
+        return -1;
     }
-    return (lo < nu && __ldg(uk + lo) == key) ? lo : -1;
+};
+
+// insert the nu unique keys (nu read on the device); a full table is impossible at load <= 1/2
+__global__ void k_hash_insert(const unsigned long long* __restrict__ ukeys, const int* __restrict__ nu_p, unsigned long long* __restrict__ hk,
+                              int* __restrict__ hv, unsigned long long mask) {
+    const int u = blockIdx.x * blockDim.x + threadIdx.x;
+    if (u >= *nu_p) return;
+    const unsigned long long key = ukeys[u];
+    unsigned long long h = mix64(key) & mask;
+    for (unsigned long long n = 0; n <= mask; ++n) {
+        const unsigned long long prev = atomicCAS(hk + h, HASH_EMPTY, key);
+        if (prev == HASH_EMPTY || prev == key) {
+            hv[h] = u;
+            return;
+        }
+        h = (h + 1) & mask;
+    }
 }
 
 // ---------------------------------------------------------------- constraint rows
@@ -177,11 +215,9 @@ __device__ void attempt_ee(const double* __restrict__ x, const double* __restric
 // one thread per boundary triangle; points hashed with mode 0
 __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
                                                  const double* __restrict__ x, double dh, double dh2, SceneGeo g,
-                                                 const unsigned long long* __restrict__ uk, const int* __restrict__ us,
-                                                 const int* __restrict__ nu_p, const int* __restrict__ ids, RowSink sink) {
+                                                 GridView gv, RowSink sink) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
-    const int nu = *nu_p;
     if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
     const int sc = g.scene(t0);
@@ -191,10 +227,10 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
+                const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = us[c]; k < us[c + 1]; ++k) {
-                    const int j = ids[k];
+                for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
+                    const int j = gv.ids[k];
                     const int p = bp[j];
                     const C3 plo = cell_of(ld3(x, p) - mk(dh, dh, dh), inv_dx);
                     const C3 first = cmax(lo, plo);
@@ -207,11 +243,9 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
 // one thread per boundary edge (query, box +- dh); stored edges hashed with mode 1
 __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
                                                  const double* __restrict__ x0, double dh, double dh2, SceneGeo g,
-                                                 const unsigned long long* __restrict__ uk, const int* __restrict__ us,
-                                                 const int* __restrict__ nu_p, const int* __restrict__ ids, RowSink sink) {
+                                                 GridView gv, RowSink sink) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbe) return;
-    const int nu = *nu_p;
     if (g.big_edge && g.big_edge[i]) return;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
     const int sc = g.scene(a0);
@@ -222,10 +256,10 @@ __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict_
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
+                const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = us[c]; k < us[c + 1]; ++k) {
-                    const int j = ids[k];
+                for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
+                    const int j = gv.ids[k];
                     if (!(i < j)) continue;
                     const int b0 = be[2 * j], b1 = be[2 * j + 1];
                     const C3 slo = cell_of(vmin(ld3(x, b0), ld3(x, b1)), inv_dx);
@@ -244,12 +278,9 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* slot, double 
 // compute_filter_3D_PT (NEWTON_IPC.py:377-406): triangles query their moving bbox
 __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
                                                 const double* __restrict__ x, const double* __restrict__ p, double dh, SceneGeo g,
-                                                double eta, const unsigned long long* __restrict__ uk, const int* __restrict__ us,
-                                                const int* __restrict__ nu_p, const int* __restrict__ ids,
-                                                unsigned long long* __restrict__ alpha) {
+                                                double eta, GridView gv, unsigned long long* __restrict__ alpha) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
-    const int nu = *nu_p;
     if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
     const int sc = g.scene(t0);
@@ -263,10 +294,10 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
+                const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = us[c]; k < us[c + 1]; ++k) {
-                    const int pp = bp[ids[k]];
+                for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
+                    const int pp = bp[gv.ids[k]];
                     if (pp == t0 || pp == t1 || pp == t2) continue;
                     const v3 P = ld3(x, pp), dP = ld3(p, pp);
                     const C3 plo = cell_of(vmin(P, P + dP) - d, inv_dx);
@@ -282,12 +313,9 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
 // compute_filter_3D_EE (NEWTON_IPC.py:409-440): edges query moving bbox +- dh
 __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
                                                 const double* __restrict__ p, double dh, SceneGeo g, double eta,
-                                                const unsigned long long* __restrict__ uk, const int* __restrict__ us,
-                                                const int* __restrict__ nu_p, const int* __restrict__ ids,
-                                                unsigned long long* __restrict__ alpha) {
+                                                GridView gv, unsigned long long* __restrict__ alpha) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbe) return;
-    const int nu = *nu_p;
     if (g.big_edge && g.big_edge[i]) return;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
     const int sc = g.scene(a0);
@@ -299,10 +327,10 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
-                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
+                const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = us[c]; k < us[c + 1]; ++k) {
-                    const int j = ids[k];
+                for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
+                    const int j = gv.ids[k];
                     if (!(i < j)) continue;
                     const int b0 = be[2 * j], b1 = be[2 * j + 1];
                     if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) continue;
@@ -332,11 +360,9 @@ __global__ void __launch_bounds__(128) k_ccd_inversion(int nT, const int4* __res
 // check_collision_3d (NEWTON_IPC.py:855-880): triangles query bbox cells, edges hashed +- dh
 __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restrict__ bt, const int* __restrict__ be,
                                                    const double* __restrict__ x, double dh, SceneGeo g,
-                                                   const unsigned long long* __restrict__ uk, const int* __restrict__ us,
-                                                   const int* __restrict__ nu_p, const int* __restrict__ ids, int* __restrict__ hit) {
+                                                   GridView gv, int* __restrict__ hit) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
-    const int nu = *nu_p;
     if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
     const int sc = g.scene(t0);
@@ -349,10 +375,10 @@ __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restric
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
                 if (*(volatile int*)hit) return;
-                const int c = find_cell(uk, nu, gkey(g, sc, cx, cy, cz));
+                const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = us[c]; k < us[c + 1]; ++k) {
-                    const int j = ids[k];
+                for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
+                    const int j = gv.ids[k];
                     const int a0 = be[2 * j], a1 = be[2 * j + 1];
                     if (a0 == t0 || a0 == t1 || a0 == t2 || a1 == t0 || a1 == t1 || a1 == t2) continue;
                     const v3 P = ld3(x, a0), Q = ld3(x, a1);
@@ -649,7 +675,27 @@ int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const dou
     if (st) return st;
     st = cub_call(c, [&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, runs, g.ustart.as<int>(), N + 1, s); });
     if (st) return st;
+    // cell table
+    unsigned long long size = 1;
+    while (size < 2ull * (unsigned long long)N) size <<= 1;
+    if (g.hkeys.ensure(8 * size) || g.hvals.ensure(4 * size)) return FIPC_ERR_CUDA;
+    FIPC_CUDA(cudaMemsetAsync(g.hkeys.p, 0xff, 8 * size, s));
+    g.hmask = size - 1;
+    k_hash_insert<<<nblk(N, 256), 256, 0, s>>>(g.ukeys.as<unsigned long long>(), nu, g.hkeys.as<unsigned long long>(), g.hvals.as<int>(),
+                                               g.hmask);
+    FIPC_LAUNCHED();
+    FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
+}
+
+static GridView view(const Grid& g) {
+    GridView v;
+    v.hk = g.hkeys.as<unsigned long long>();
+    v.hv = g.hvals.as<int>();
+    v.mask = g.hmask;
+    v.us = g.ustart.as<int>();
+    v.ids = g.ids.as<int>();
+    return v;
 }
 
 // sort + unique each list in place (rows_tmp as staging); returns counts in c->h_counts
@@ -725,8 +771,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         if (st) return st;
         if (c->gp.n_entries > 0 && c->nBT > 0) {
             k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, sg,
-                                                         c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
-                                                         c->gp.ncells.as<int>(), c->gp.ids.as<int>(), sink);
+                                                         view(c->gp), sink);
             FIPC_LAUNCHED();
         }
         if (c->nBT > 0 && c->nBP > 0) {
@@ -737,8 +782,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         if (st) return st;
         if (c->ge.n_entries > 0) {
             k_find_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, sg,
-                                                         c->ge.ukeys.as<unsigned long long>(), c->ge.ustart.as<int>(),
-                                                         c->ge.ncells.as<int>(), c->ge.ids.as<int>(), sink);
+                                                         view(c->ge), sink);
             FIPC_LAUNCHED();
         }
         if (c->nBE > 1) {
@@ -771,8 +815,7 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     if (st) return st;
     if (c->gp.n_entries > 0 && c->nBT > 0) {
         k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, sg, eta,
-                                                    c->gp.ukeys.as<unsigned long long>(), c->gp.ustart.as<int>(),
-                                                    c->gp.ncells.as<int>(), c->gp.ids.as<int>(), slot);
+                                                    view(c->gp), slot);
         FIPC_LAUNCHED();
     }
     if (c->nBT > 0 && c->nBP > 0) {
@@ -782,8 +825,7 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     st = build_grid(c, c->ge, 3, c->nBE, c->be, x, p, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0) {
-        k_ccd_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, c->ge.ukeys.as<unsigned long long>(),
-                                                    c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), slot);
+        k_ccd_ee<<<nblk(c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, view(c->ge), slot);
         FIPC_LAUNCHED();
     }
     if (c->nBE > 1) {
@@ -821,8 +863,7 @@ int collision_launch(fipc_ctx* c, const double* x, int* hit, cudaStream_t s) {
     st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0 && c->nBT > 0) {
-        k_collision<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, sg, c->ge.ukeys.as<unsigned long long>(),
-                                                       c->ge.ustart.as<int>(), c->ge.ncells.as<int>(), c->ge.ids.as<int>(), hit);
+        k_collision<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, sg, view(c->ge), hit);
         FIPC_LAUNCHED();
     }
     if (c->nBT > 0 && c->nBE > 0) {

@@ -69,7 +69,8 @@ void free_ctx(fipc_ctx* c) {
     for (DBuf* b : bufs) b->release();
     Grid* gs[] = {&c->gp, &c->ge};
     for (Grid* g : gs) {
-        DBuf* gb[] = {&g->keys, &g->ids, &g->keys_alt, &g->ids_alt, &g->ukeys, &g->ustart, &g->counts, &g->offsets, &g->ncells, &g->tmp};
+        DBuf* gb[] = {&g->keys, &g->ids, &g->keys_alt, &g->ids_alt, &g->ukeys, &g->ustart, &g->counts, &g->offsets, &g->ncells, &g->tmp,
+                      &g->hkeys, &g->hvals};
         for (DBuf* b : gb) b->release();
     }
     delete c;

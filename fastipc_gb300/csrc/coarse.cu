@@ -133,38 +133,108 @@ __global__ void k_cs_regularize(int n, double* __restrict__ Ac) {
     *dk = *dk > 0.0 ? *dk * (1.0 + 1e-12) : 1.0;
 }
 
-// in-place Gauss-Jordan inverse of the SPD matrix A (n x n, no pivoting needed); one
-// cooperative launch, one grid barrier per pivot.  buf: 4n doubles (pivot row / column, double
-// buffered: the threads that write row and column k+1 during step k stage them for step k+1)
-__global__ void k_cs_gauss_jordan(int n, double* __restrict__ A, double* __restrict__ buf) {
+// In-place blocked Gauss-Jordan inverse of the SPD matrix A (n x n, n a multiple of GJ_B; no
+// pivoting is needed: every diagonal block met is a diagonal block of a Schur complement of an
+// SPD matrix).  One cooperative launch; per block column K three phases separated by grid
+// barriers:
+//   1. T = A_KK^-1 (one CTA, Gauss-Jordan in shared memory); every CTA copies column panel C = A_*K
+//   2. R = T A_K*                                   (row panel)
+//   3. A_KK = T, A_KJ = R_J, A_IK = -C_I T, A_IJ -= C_I R_J   (32 x 32 tiles in shared memory)
+// buf: T (B^2) + C (n B) + R (B n) doubles.
+constexpr int GJ_B = 32, GJ_THREADS = 256;
+__global__ void __launch_bounds__(GJ_THREADS) k_cs_gauss_jordan(int n, double* __restrict__ A, double* __restrict__ buf) {
     cg::grid_group grid = cg::this_grid();
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x, nthr = (long long)gridDim.x * blockDim.x;
-    const long long nn = (long long)n * n;
-    double* bc[2] = {buf, buf + 2 * n};
-    double* br[2] = {buf + n, buf + 3 * n};
-    for (long long e = tid; e < n; e += nthr) {
-        bc[0][e] = A[e * n];
-        br[0][e] = A[e];
-    }
-    grid.sync();
-    for (int k = 0; k < n; ++k) {
-        const double* col = bc[k & 1];
-        const double* row = br[k & 1];
-        double* ncol = bc[(k + 1) & 1];
-        double* nrow = br[(k + 1) & 1];
-        const double inv = 1.0 / row[k];
-        for (long long e = tid; e < nn; e += nthr) {
-            const int i = (int)(e / n), j = (int)(e - (long long)i * n);
-            double v;
-            if (i == k) v = (j == k) ? inv : row[j] * inv;
-            else if (j == k) v = -col[i] * inv;
-            else v = A[e] - col[i] * row[j] * inv;
-            A[e] = v;
-            if (j == k + 1) ncol[i] = v;
-            if (i == k + 1) nrow[j] = v;
+    __shared__ double sa[GJ_B][GJ_B + 1];
+    __shared__ double sb[GJ_B][GJ_B + 1];
+    __shared__ double piv[GJ_B], pcol[GJ_B];
+    const int nb = n / GJ_B, t = threadIdx.x;
+    const long long gtid = (long long)blockIdx.x * GJ_THREADS + t, gthr = (long long)gridDim.x * GJ_THREADS;
+    double* T = buf;
+    double* C = buf + GJ_B * GJ_B;
+    double* R = C + (size_t)n * GJ_B;
+    for (int K = 0; K < nb; ++K) {
+        const int k0 = K * GJ_B;
+        // phase 1
+        if (blockIdx.x == 0) {
+            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) sa[e / GJ_B][e % GJ_B] = A[(size_t)(k0 + e / GJ_B) * n + k0 + e % GJ_B];
+            __syncthreads();
+            for (int k = 0; k < GJ_B; ++k) {
+                if (t < GJ_B) {
+                    piv[t] = sa[k][t];
+                    pcol[t] = sa[t][k];
+                }
+                __syncthreads();
+                const double inv = 1.0 / piv[k];
+                for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
+                    const int i = e / GJ_B, j = e % GJ_B;
+                    double v;
+                    if (i == k) v = (j == k) ? inv : piv[j] * inv;
+                    else if (j == k) v = -pcol[i] * inv;
+                    else v = sa[i][j] - pcol[i] * piv[j] * inv;
+                    sa[i][j] = v;
+                }
+                __syncthreads();
+            }
+            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) T[e] = sa[e / GJ_B][e % GJ_B];
+        }
+        for (long long e = gtid; e < (long long)n * GJ_B; e += gthr) {
+            const int i = (int)(e / GJ_B), m = (int)(e % GJ_B);
+            C[e] = A[(size_t)i * n + k0 + m];
+        }
+        grid.sync();
+        // phase 2: R[k][j] = sum_m T[k][m] A[k0 + m][j]
+        for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) sb[e / GJ_B][e % GJ_B] = T[e];
+        __syncthreads();
+        for (long long e = gtid; e < (long long)n * GJ_B; e += gthr) {
+            const int k = (int)(e / n), j = (int)(e % n);
+            double v = 0.0;
+#pragma unroll 8
+            for (int m = 0; m < GJ_B; ++m) v += sb[k][m] * A[(size_t)(k0 + m) * n + j];
+            R[(size_t)k * n + j] = v;
+        }
+        grid.sync();
+        // phase 3, one 32 x 32 tile per CTA iteration
+        for (int tile = blockIdx.x; tile < nb * nb; tile += gridDim.x) {
+            const int I = tile / nb, J = tile % nb, i0 = I * GJ_B, j0 = J * GJ_B;
+            __syncthreads();
+            // sa = C_I (rows i0.., 32 columns); sb = R_J or T
+            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
+                const int r = e / GJ_B, c = e % GJ_B;
+                sa[r][c] = C[(size_t)(i0 + r) * GJ_B + c];
+                sb[r][c] = (J == K) ? T[r * GJ_B + c] : R[(size_t)r * n + j0 + c];
+            }
+            __syncthreads();
+            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
+                const int r = e / GJ_B, c = e % GJ_B;
+                double* out = A + (size_t)(i0 + r) * n + j0 + c;
+                if (I == K) {
+                    *out = sb[r][c];            // T on the diagonal tile, R_J elsewhere
+                } else {
+                    double v = 0.0;
+#pragma unroll 8
+                    for (int m = 0; m < GJ_B; ++m) v += sa[r][m] * sb[m][c];
+                    *out = (J == K) ? -v : *out - v;
+                }
+            }
         }
         grid.sync();
     }
+}
+
+// cooperative launch of the inverse over a grid that fits the GPU (n a multiple of GJ_B)
+static int launch_gauss_jordan(int n, double* A, double* buf, cudaStream_t s) {
+    int dev = 0, nsm = 0, per = 0;
+    FIPC_CUDA(cudaGetDevice(&dev));
+    FIPC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    FIPC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cs_gauss_jordan, GJ_THREADS, 0));
+    if (per < 1) return FIPC_ERR_CUDA;
+    int grid = nsm * (per < 2 ? per : 2);
+    const int tiles = (n / GJ_B) * (n / GJ_B);
+    if (grid > tiles) grid = tiles;
+    void* args[] = {&n, &A, &buf};
+    FIPC_CUDA(cudaLaunchCooperativeKernel((const void*)k_cs_gauss_jordan, dim3(grid), dim3(GJ_THREADS), args, 0, s));
+    FIPC_LAUNCHED();
+    return FIPC_OK;
 }
 
 // u_i += P_i y_I = y_t + y_w x d_i on free vertices, y_I = rows 6I..6I+5 of Ac^-1 times g: each
@@ -175,7 +245,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_cs_prolong(PCGArgs a) {
     const int I = blockIdx.x / a.cs_blocks;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int k = wid; k < 6; k += PCG_THREADS / 32) {
-        const double* Ar = a.cs_ainv + (size_t)(6 * I + k) * a.cs_n;
+        const double* Ar = a.cs_ainv + (size_t)(6 * I + k) * a.cs_ld;
         double t = 0.0;
         for (int j = lane; j < a.cs_n; j += 32) t += __ldg(Ar + j) * __ldg(a.cs_g + j);
 #pragma unroll
@@ -238,30 +308,20 @@ int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
     a.cs_blocks = 0;
     if (!c->cs_agg_rows) return FIPC_OK;
     const int n = 6 * c->cs_n_agg, nb = nblk_c(c->nV, PCG_THREADS);
-    if (c->cs_Ac.ensure(8ll * n * n) || c->cs_buf.ensure(8ll * 4 * n) || c->cs_part.ensure(48ll * nb) || c->cs_gbuf.ensure(8ll * n) ||
-        c->cs_tick.ensure(4ll * c->cs_n_agg))
+    const int ld = ((n + GJ_B - 1) / GJ_B) * GJ_B;   // padded with identity rows to whole GJ blocks
+    if (c->cs_Ac.ensure(8ll * ld * ld) || c->cs_buf.ensure(8ll * (GJ_B * GJ_B + 2ll * ld * GJ_B)) || c->cs_part.ensure(48ll * nb) ||
+        c->cs_gbuf.ensure(8ll * n) || c->cs_tick.ensure(4ll * c->cs_n_agg))
         return FIPC_ERR_CUDA;
     FIPC_CUDA(cudaMemsetAsync(c->cs_tick.p, 0, 4ll * c->cs_n_agg, s));   // aggregate tickets
     double* Ac = c->cs_Ac.as<double>();
-    FIPC_CUDA(cudaMemsetAsync(Ac, 0, 8ll * n * n, s));
-    k_cs_build<<<c->cs_n_pairs, CS_BUILD_THREADS, 0, s>>>(c->nV, c->cs_agg_rows, n, c->cs_pairs, c->sell_off, c->sell_col, c->row_len,
-                                                    c->sell_val, fixed, c->cs_d.as<double>(), Ac);
+    FIPC_CUDA(cudaMemsetAsync(Ac, 0, 8ll * ld * ld, s));
+    k_cs_build<<<c->cs_n_pairs, CS_BUILD_THREADS, 0, s>>>(c->nV, c->cs_agg_rows, ld, c->cs_pairs, c->sell_off, c->sell_col, c->row_len,
+                                                          c->sell_val, fixed, c->cs_d.as<double>(), Ac);
     FIPC_LAUNCHED();
-    k_cs_regularize<<<nblk_c(n, 128), 128, 0, s>>>(n, Ac);
+    k_cs_regularize<<<nblk_c(ld, 128), 128, 0, s>>>(ld, Ac);
     FIPC_LAUNCHED();
-    int dev = 0, nsm = 0, per = 0;
-    FIPC_CUDA(cudaGetDevice(&dev));
-    FIPC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    FIPC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cs_gauss_jordan, 256, 0));
-    if (per < 1) return FIPC_ERR_CUDA;
-    int grid = nsm * (per < 2 ? per : 2);
-    const long long need = ((long long)n * n + 255) / 256;
-    if (grid > need) grid = (int)(need > 0 ? need : 1);
-    int nn = n;
-    double* buf = c->cs_buf.as<double>();
-    void* args[] = {&nn, &Ac, &buf};
-    FIPC_CUDA(cudaLaunchCooperativeKernel((const void*)k_cs_gauss_jordan, dim3(grid), dim3(256), args, 0, s));
-    FIPC_LAUNCHED();
+    int st = launch_gauss_jordan(ld, Ac, c->cs_buf.as<double>(), s);
+    if (st) return st;
     a.cs_blocks = c->cs_agg_rows / PCG_THREADS;
     a.cs_d = c->cs_d.as<double>();
     a.cs_part = c->cs_part.as<double>();
@@ -269,6 +329,7 @@ int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
     a.cs_ticket = c->cs_tick.as<int>();
     a.cs_ainv = Ac;
     a.cs_n = n;
+    a.cs_ld = ld;
     FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
 }
@@ -287,3 +348,14 @@ void cs_free(fipc_ctx* c) {
 }
 
 }  // namespace fipc
+
+using namespace fipc;
+
+// in-place inverse of a dense SPD matrix (n a multiple of 32, row-major); work: 1024 + 64 n doubles
+extern "C" int fipc_dense_spd_inverse(int n, double* A, double* work, void* stream) {
+    if (n <= 0 || n % GJ_B || !A || !work) return FIPC_ERR_ARGUMENT;
+    const int st = launch_gauss_jordan(n, A, work, (cudaStream_t)stream);
+    if (st) return st;
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}

@@ -53,8 +53,9 @@ struct DBuf {
 // sorted spatial-hash grid over primitives: (cell key, primitive id) pairs sorted by key,
 // unique keys and the start of each key's run
 struct Grid {
-    DBuf keys, ids, keys_alt, ids_alt, ukeys, ustart, counts, offsets, ncells, tmp;
+    DBuf keys, ids, keys_alt, ids_alt, ukeys, ustart, counts, offsets, ncells, tmp, hkeys, hvals;
     int n_entries = 0, n_unique = 0;
+    unsigned long long hmask = 0;   // cell table size - 1 (a power of two >= 2 x entries)
 };
 
 struct fipc_ctx_impl {
@@ -153,10 +154,11 @@ FIPC_HD unsigned long long cell_key(long long i, long long j, long long k) {
     auto c = [](long long v) { return v < 0 ? 0ll : (v > (1ll << 21) - 1 ? (1ll << 21) - 1 : v); };
     return ((unsigned long long)c(i + off) << 42) | ((unsigned long long)c(j + off) << 21) | (unsigned long long)c(k + off);
 }
-// batched scenes: 10 bits of scene id above 18 bits per axis (offset 2^17)
+// batched scenes: 10 bits of scene id above 18 bits per axis (offset 2^17; the top coordinate
+// value is never used, so no key is all ones)
 FIPC_HD unsigned long long cell_key_scene(int s, long long i, long long j, long long k) {
     const long long off = 1ll << 17;
-    auto c = [](long long v) { return v < 0 ? 0ll : (v > (1ll << 18) - 1 ? (1ll << 18) - 1 : v); };
+    auto c = [](long long v) { return v < 0 ? 0ll : (v > (1ll << 18) - 2 ? (1ll << 18) - 2 : v); };
     return ((unsigned long long)s << 54) | ((unsigned long long)c(i + off) << 36) | ((unsigned long long)c(j + off) << 18) |
            (unsigned long long)c(k + off);
 }

@@ -24,8 +24,8 @@ struct PCGArgs {
     double* cs_part;                 // [nblk][6] per-block restriction (force, torque) of r
     double* cs_g;                    // [6 n_agg] restriction per aggregate
     int* cs_ticket;                  // [n_agg] blocks of the aggregate done (reset by its last block)
-    const double* cs_ainv;           // [6 n_agg]^2 inverse coarse matrix
-    int cs_n;                        // 6 n_agg
+    const double* cs_ainv;           // inverse coarse matrix, row stride cs_ld
+    int cs_n, cs_ld;                 // 6 n_agg; padded row stride
 };
 enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
 constexpr int PCG_THREADS = 128;
@@ -96,12 +96,34 @@ __device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double*
     }
 }
 
+// block sums of NV per-thread values into the shared array out[NV] (valid in every thread on
+// return).  The values go through shared memory and warp c sums component c (four rows per lane,
+// then a shuffle tree), so the block spends about 8 FP64 adds per component per lane of one warp
+// instead of a full shuffle tree in every warp; the order is fixed.
+template <int NV>
+__device__ __forceinline__ void block_sums(const double (&v)[NV], double* out) {
+    __shared__ double sv[NV][PCG_THREADS];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) sv[c][threadIdx.x] = v[c];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int c = wid; c < NV; c += PCG_THREADS / 32) {
+        double x = sv[c][lane];
+#pragma unroll
+        for (int k = 1; k < PCG_THREADS / 32; ++k) x += sv[c][lane + 32 * k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) out[c] = x;
+    }
+    __syncthreads();
+}
+
 // restriction of one block's residuals onto the rigid-body modes of its aggregate: the block's
 // sum over rows of (r_i, d_i x r_i) into cs_part[block] (fixed shuffle / shared order); the
 // aggregate's last block to finish (atomic ticket) sums its blocks' partials in block order
 // into cs_g, so the aggregate totals need no extra launch and are reproducible
 __device__ __forceinline__ void block_restrict(const PCGArgs& a, bool valid, int i, const double (&r)[3], const double (&d)[3]) {
-    __shared__ double sh[6][PCG_THREADS / 32];
+    __shared__ double tot[6];
     __shared__ bool last;
     double v[6] = {0, 0, 0, 0, 0, 0};
     if (valid) {
@@ -112,20 +134,10 @@ __device__ __forceinline__ void block_restrict(const PCGArgs& a, bool valid, int
         v[4] = d[2] * r[0] - d[0] * r[2];
         v[5] = d[0] * r[1] - d[1] * r[0];
     }
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        double x = v[c];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[c][wid] = x;
-    }
-    __syncthreads();
+    block_sums<6>(v, tot);
     const int I = blockIdx.x / a.cs_blocks;
     if (threadIdx.x < 6) {
-        double t = 0.0;
-        for (int k = 0; k < PCG_THREADS / 32; ++k) t += sh[threadIdx.x][k];
-        a.cs_part[6 * (size_t)blockIdx.x + threadIdx.x] = t;
+        a.cs_part[6 * (size_t)blockIdx.x + threadIdx.x] = tot[threadIdx.x];
         __threadfence();
     }
     __syncthreads();

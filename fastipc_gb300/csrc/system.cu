@@ -180,24 +180,12 @@ __global__ void k_contact_rowptr(int nV, int nu, const unsigned long long* __res
 // the last block to finish, which then reduces the partials with final_sums
 template <int NV>
 __device__ __forceinline__ bool block_partials(const PCGArgs& a, const double (&v)[NV]) {
-    __shared__ double sh[NV][PCG_THREADS / 32];
+    __shared__ double tot[NV];
     __shared__ bool last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int c = 0; c < NV; ++c) {
-        double x = v[c];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[c][wid] = x;
-    }
-    __syncthreads();
+    block_sums<NV>(v, tot);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < NV; ++c) {
-            double t = 0.0;
-            for (int k = 0; k < PCG_THREADS / 32; ++k) t += sh[c][k];
-            a.part[c * gridDim.x + blockIdx.x] = t;
-        }
+        for (int c = 0; c < NV; ++c) a.part[c * gridDim.x + blockIdx.x] = tot[c];
         __threadfence();
         const int ticket = atomicAdd(&a.flag[2], 1);
         last = ticket == (int)gridDim.x - 1;

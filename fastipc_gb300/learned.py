@@ -40,8 +40,9 @@ def _p(t):
 class WarmStartMLP:
     IN, H, OUT = 64, 128, 4
 
-    def __init__(self, device='cuda:0', seed=0, params=None, scale=1.0):
+    def __init__(self, device='cuda:0', seed=0, params=None, scale=1.0, rest_relative=True):
         self.scale = float(scale)
+        self.rest_relative = bool(rest_relative)   # the feature mode it was trained with
         self.device = torch.device(device)
         self.nparam = int(N.lib().fipc_mlp_param_count())
         if params is None:
@@ -87,12 +88,13 @@ class WarmStartMLP:
         return self.loss
 
     def save(self, path):
-        np.savez(path, params=self.params.cpu().numpy(), scale=np.float64(self.scale))
+        np.savez(path, params=self.params.cpu().numpy(), scale=np.float64(self.scale), rest_relative=np.int32(self.rest_relative))
 
     @classmethod
     def load(cls, path, device='cuda:0'):
         d = np.load(path)
-        return cls(device=device, params=torch.from_numpy(d['params']), scale=float(d['scale']))
+        return cls(device=device, params=torch.from_numpy(d['params']), scale=float(d['scale']),
+                   rest_relative=bool(d['rest_relative']) if 'rest_relative' in d else False)
 
 
 def _init_params(seed):
@@ -155,7 +157,7 @@ class LearnedStart:
         if self._X is None or self._X.shape[0] != sim.nV:
             self._X = torch.empty((sim.nV, WarmStartMLP.IN), dtype=F32, device=sim.device)
             self._tmp = torch.empty((sim.nV, 3), dtype=torch.float64, device=sim.device)
-        X = features(sim, self._X)
+        X = features(sim, self._X, self.model.rest_relative)
         out = self.model.forward(X)
         corr = torch.where((sim.fixed == 0).unsqueeze(1), out[:, :3].to(torch.float64) * (self.model.scale / sim.inv_dx),
                            torch.zeros_like(d0)).contiguous()
@@ -204,24 +206,25 @@ class LearnedStart:
 class _Recorder:
     """Hook that records (features, free mask, inertial predictor) at each step's start."""
 
-    def __init__(self, inner=None):
+    def __init__(self, inner=None, rest_relative=True):
         self.pending = None
         self.inner = inner
+        self.rest_relative = rest_relative
 
     def __call__(self, sim, f):
         sim.find_constraints()
-        self.pending = (features(sim).clone(), (sim.fixed == 0).clone(), sim.xTilde.clone())
+        self.pending = (features(sim, rest_relative=self.rest_relative).clone(), (sim.fixed == 0).clone(), sim.xTilde.clone())
         if self.inner is not None:
             self.inner(sim, f)
 
 
-def collect(scene, steps, device='cuda:0', pcg_rtol=1e-6, start=0):
+def collect(scene, steps, device='cuda:0', pcg_rtol=1e-6, start=0, rest_relative=True):
     """Run the solver (inertial start, which converges to the same steps as the plain one) for
     ``steps`` steps; returns (X [n,64], Y [n,4]) over the free vertices of steps >= start,
     Y = (x^{n+1} - xTilde) / h."""
     from .newton import NewtonIPC
     sim = NewtonIPC(scene, device=device, pcg_rtol=pcg_rtol)
-    rec = _Recorder(LearnedStart(kind='inertial'))
+    rec = _Recorder(LearnedStart(kind='inertial'), rest_relative=rest_relative)
     sim.initial_guess = rec
     h = 1.0 / sim.inv_dx
     Xs, Ys = [], []
@@ -298,12 +301,12 @@ def _split(X, Y, seed=0):
     return X[perm[nval:]].contiguous(), Y[perm[nval:]].contiguous(), X[perm[:nval]].contiguous(), Y[perm[:nval]].contiguous()
 
 
-def fit(X, Y, device='cuda:0', epochs=30, log=print, seed=0):
+def fit(X, Y, device='cuda:0', epochs=30, log=print, seed=0, rest_relative=True):
     """Train a model on (X, Y in h units); the target scale is the RMS of Y.  Returns the model
     and its statistics (validation MSE of the network and of the inertial guess, in h^2)."""
     Xt, Yt, Xv, Yv = _split(X, Y, seed)
     scale = float(Yt[:, :3].pow(2).mean().sqrt())
-    model = WarmStartMLP(device, seed=seed, scale=scale)
+    model = WarmStartMLP(device, seed=seed, scale=scale, rest_relative=rest_relative)
     t1 = time.perf_counter()
     hist = train(model, Xt, Yt / scale, epochs=epochs, log=log)
     torch.cuda.synchronize()
@@ -313,107 +316,108 @@ def fit(X, Y, device='cuda:0', epochs=30, log=print, seed=0):
     return model, stats
 
 
-def _small_train_scenes():
+def collect_bar(nx, seed, steps, device='cuda:0', rest_relative=True, pcg_rtol=1e-6):
+    """Transitions of the twisted bar (20 x 20 cross-section, nx hexes long) with the inertial start."""
     from . import scenes as S
-    out = [(S.twisted_bar(nx=100, ny=6, nz=6, seed=s, speed=sp), 60) for s, sp in [(0, np.pi), (1, 0.5 * np.pi), (2, 1.5 * np.pi)]]
-    out += [(S.two_cubes(n=6, seed=s), 40) for s in range(4)]
-    out += [(S.cube_lattice(m=2, n=4, seed=s), 40) for s in range(6)]
-    return out
+    sc = S.twisted_bar(nx=nx, ny=20, nz=20, size=(nx / 400.0, 0.05, 0.05), seed=seed)
+    return collect(sc, steps, device, pcg_rtol, rest_relative=rest_relative)
 
 
-def _small_test_scenes():
-    from . import scenes as S
-    return [('twisted_bar_200x10x10', S.twisted_bar(nx=200, ny=10, nz=10, seed=7), 40),
-            ('two_cubes_n8', S.two_cubes(n=8, seed=11), 40),
-            ('cube_lattice_8_seed20', S.cube_lattice(m=2, n=4, seed=20), 40),
-            ('cube_lattice_8_seed21', S.cube_lattice(m=2, n=4, seed=21), 40)]
-
-
-def experiment_small(out_dir, device='cuda:0', epochs=30, log=print):
-    """Train on small seed-varied scenes, compare plain / inertial / MLP starts on unseen ones."""
-    import os
-    os.makedirs(out_dir, exist_ok=True)
-    t0 = time.perf_counter()
-    Xs, Ys = [], []
-    for sc, steps in _small_train_scenes():
-        X, Y = collect(sc, steps, device)
-        Xs.append(X)
-        Ys.append(Y)
-        log(f'collected {sc.name} {sc.meta}: {X.shape[0]} rows')
-    res = {'collect_s': time.perf_counter() - t0}
-    model, stats = fit(torch.cat(Xs), torch.cat(Ys), device, epochs, log)
-    res.update(stats)
-    model.save(os.path.join(out_dir, 'warmstart_small.npz'))
-    res['scenes'] = {}
-    for name, sc, steps in _small_test_scenes():
-        r = {}
-        xs = {}
-        for mode in ('plain', 'inertial', 'mlp'):
-            guess = None if mode == 'plain' else LearnedStart(model if mode == 'mlp' else None, kind=mode)
-            r[mode], xs[mode] = run_scene(sc, steps, guess, device)
-        for mode in ('inertial', 'mlp'):
-            r[mode]['max_dev_vs_plain'] = float(np.abs(xs[mode] - xs['plain']).max())
-        res['scenes'][name] = r
-        log(f"{name}: newton plain {r['plain']['newton']} inertial {r['inertial']['newton']} mlp {r['mlp']['newton']}; "
-            f"wall {r['plain']['wall_s']:.2f} / {r['inertial']['wall_s']:.2f} / {r['mlp']['wall_s']:.2f} s")
-    with open(os.path.join(out_dir, 'warmstart_small.json'), 'w') as fh:
-        json.dump(res, fh, indent=1)
-    return res
-
-
-def experiment_bar(out_dir, nx=400, train_steps=30, eval_steps=30, device='cuda:0', epochs=20, log=print, pcg_rtol=1e-6):
-    """The twisted bar with its own transitions: collect steps [0, train_steps) with the
-    inertial start, train, then run steps [train_steps, train_steps + eval_steps) from the same
-    state with the plain, inertial and learned starts."""
-    import os
-    from . import scenes as S
-    from .newton import NewtonIPC
-    os.makedirs(out_dir, exist_ok=True)
-    sc = S.twisted_bar(nx=nx, ny=20, nz=20, size=(nx / 400.0, 0.05, 0.05), seed=0)
-    sim = NewtonIPC(sc, device=device, pcg_rtol=pcg_rtol)
-    rec = _Recorder(LearnedStart(kind='inertial'))
-    sim.initial_guess = rec
-    h = 1.0 / sim.inv_dx
-    Xs, Ys = [], []
-    t0 = time.perf_counter()
-    for f in range(train_steps):
-        sim.step(f)
-        X, free, xt = rec.pending
-        Y = torch.zeros((sim.nV, 4), dtype=F32, device=sim.device)
-        Y[:, :3] = ((sim.x - xt) / h).to(F32)
-        Xs.append(X[free])
-        Ys.append(Y[free])
-    res = {'scene': sc.meta, 'train_steps': train_steps, 'eval_steps': eval_steps, 'collect_s': time.perf_counter() - t0}
-    model, stats = fit(torch.cat(Xs), torch.cat(Ys), device, epochs, log)
-    del Xs, Ys
-    res.update(stats)
-    model.save(os.path.join(out_dir, f'warmstart_bar{nx}.npz'))
+def compare_starts(sim, steps, f0, modes, log=print):
+    """Run steps [f0, f0 + steps) from sim's current state once per mode (the state is restored
+    between modes).  modes: name -> None (plain) or a LearnedStart."""
     snap = (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone())
-    xs = {}
-    modes = {'plain': None, 'inertial': ('inertial', 0), 'mlp': ('mlp', 0), 'mlp_s2': ('mlp', 2), 'mlp_s4': ('mlp', 4),
-             'mlp_s8': ('mlp', 8)}
-    for mode, spec in modes.items():
+    out, xs = {}, {}
+    for name, guess in modes.items():
         sim.x.copy_(snap[0])
         sim.v.copy_(snap[1])
         sim.dx_prev.copy_(snap[2])
         sim.newton_iters, sim.pcg_iters = [], []
-        guess = None if spec is None else LearnedStart(model if spec[0] == 'mlp' else None, kind=spec[0], smooth=spec[1])
         sim.initial_guess = guess
         inter = 0
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        for f in range(train_steps, train_steps + eval_steps):
+        for f in range(f0, f0 + steps):
             sim.step(f)
             inter += int(sim.check_collision())
         torch.cuda.synchronize()
-        res[mode] = _result(sim, guess, eval_steps, time.perf_counter() - t1, inter)
-        xs[mode] = sim.x.cpu().numpy()
-        log(f"bar {mode}: newton {res[mode]['newton']} pcg {res[mode]['pcg']} wall {res[mode]['wall_s']:.2f} s")
-    for mode in modes:
-        if mode != 'plain':
-            res[mode]['max_dev_vs_plain'] = float(np.abs(xs[mode] - xs['plain']).max())
+        out[name] = _result(sim, guess, steps, time.perf_counter() - t1, inter)
+        xs[name] = sim.x.cpu().numpy()
+        if log:
+            log(f"{name}: newton {out[name]['newton']} pcg {out[name]['pcg']} wall {out[name]['wall_s']:.2f} s")
+    first = next(iter(xs))
+    for name in out:
+        out[name]['max_dev_vs_' + first] = float(np.abs(xs[name] - xs[first]).max())
+    sim.initial_guess = None
+    return out
+
+
+def experiment_bar(out_dir, nx=400, train_seed=1, train_steps=80, eval_seed=0, eval_start=20, eval_steps=40, device='cuda:0',
+                   epochs=15, rest_relative=True, log=print, pcg_rtol=1e-6):
+    """Train on the transitions of one twisted bar (jitter seed train_seed) and compare plain /
+    inertial / learned starts on another (eval_seed), over steps [eval_start, eval_start +
+    eval_steps) from one state."""
+    import os
+    from . import scenes as S
+    from .newton import NewtonIPC
+    os.makedirs(out_dir, exist_ok=True)
+    t0 = time.perf_counter()
+    X, Y = collect_bar(nx, train_seed, train_steps, device, rest_relative, pcg_rtol)
+    res = {'nx': nx, 'train_seed': train_seed, 'train_steps': train_steps, 'eval_seed': eval_seed, 'eval_start': eval_start,
+           'eval_steps': eval_steps, 'rest_relative': rest_relative, 'collect_s': time.perf_counter() - t0}
+    model, stats = fit(X, Y, device, epochs, log, rest_relative=rest_relative)
+    del X, Y
+    res.update(stats)
+    tag = 'rr' if rest_relative else 'cur'
+    model.save(os.path.join(out_dir, f'warmstart_bar{nx}_{tag}.npz'))
+    sc = S.twisted_bar(nx=nx, ny=20, nz=20, size=(nx / 400.0, 0.05, 0.05), seed=eval_seed)
+    sim = NewtonIPC(sc, device=device, pcg_rtol=pcg_rtol)
+    sim.initial_guess = LearnedStart(kind='inertial')
+    for f in range(eval_start):
+        sim.step(f)
+    modes = {'plain': None, 'inertial': LearnedStart(kind='inertial')}
+    for k in (0, 2, 4, 8):
+        modes[f'mlp_s{k}'] = LearnedStart(model, kind='mlp', smooth=k)
+    res['eval'] = compare_starts(sim, eval_steps, eval_start, modes, log)
     sim.close()
-    with open(os.path.join(out_dir, f'warmstart_bar{nx}.json'), 'w') as fh:
+    with open(os.path.join(out_dir, f'warmstart_bar{nx}_{tag}.json'), 'w') as fh:
+        json.dump(res, fh, indent=1)
+    return res
+
+
+def experiment_drops(out_dir, n_train=40, n_eval=10, steps=30, m=2, n=4, device='cuda:0', epochs=15, rest_relative=True,
+                     smooth=4, log=print, pcg_rtol=1e-6):
+    """Lattice drops in the style of the 216-cube configuration (m^3 cubes of n^3 hexes over a
+    ground box): train on seeds [0, n_train), compare starts on seeds [1000, 1000 + n_eval)."""
+    import os
+    from . import scenes as S
+    from .newton import NewtonIPC
+    os.makedirs(out_dir, exist_ok=True)
+    t0 = time.perf_counter()
+    Xs, Ys = [], []
+    for seed in range(n_train):
+        X, Y = collect(S.cube_lattice(m=m, n=n, seed=seed), steps, device, pcg_rtol, rest_relative=rest_relative)
+        Xs.append(X)
+        Ys.append(Y)
+    res = {'m': m, 'n': n, 'n_train': n_train, 'n_eval': n_eval, 'steps': steps, 'rest_relative': rest_relative,
+           'transitions': n_train * steps, 'collect_s': time.perf_counter() - t0}
+    model, stats = fit(torch.cat(Xs), torch.cat(Ys), device, epochs, log, rest_relative=rest_relative)
+    del Xs, Ys
+    res.update(stats)
+    model.save(os.path.join(out_dir, f'warmstart_drops_m{m}n{n}.npz'))
+    tot = {}
+    for seed in range(1000, 1000 + n_eval):
+        sim = NewtonIPC(S.cube_lattice(m=m, n=n, seed=seed), device=device, pcg_rtol=pcg_rtol)
+        r = compare_starts(sim, steps, 0, {'plain': None, 'inertial': LearnedStart(kind='inertial'),
+                                           'mlp': LearnedStart(model, kind='mlp', smooth=smooth)}, log=None)
+        sim.close()
+        for k, v in r.items():
+            t = tot.setdefault(k, {'newton': 0, 'pcg': 0, 'wall_s': 0.0, 'intersecting_steps': 0})
+            for q in t:
+                t[q] += v[q]
+        log(f"seed {seed}: " + ', '.join(f"{k} {v['newton']}" for k, v in r.items()))
+    res['eval'] = tot
+    with open(os.path.join(out_dir, f'warmstart_drops_m{m}n{n}.json'), 'w') as fh:
         json.dump(res, fh, indent=1)
     return res
 
@@ -422,16 +426,23 @@ def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser(description='train and evaluate the learned Newton warm start')
     ap.add_argument('--out', default='warmstart_out')
-    ap.add_argument('--epochs', type=int, default=30)
-    ap.add_argument('--small', action='store_true', help='seed-varied small scenes')
+    ap.add_argument('--epochs', type=int, default=15)
     ap.add_argument('--bar', type=int, default=0, help='twisted bar with nx hexes along its axis (0: skip)')
-    ap.add_argument('--train-steps', type=int, default=30)
-    ap.add_argument('--eval-steps', type=int, default=30)
+    ap.add_argument('--train-seed', type=int, default=1)
+    ap.add_argument('--train-steps', type=int, default=80)
+    ap.add_argument('--eval-start', type=int, default=20)
+    ap.add_argument('--eval-steps', type=int, default=40)
+    ap.add_argument('--current-relative', action='store_true', help='one-ring offsets x_j - x_i instead of rest-relative')
+    ap.add_argument('--drops', type=int, default=0, help='lattice drops: number of training seeds (0: skip)')
+    ap.add_argument('--drop-eval', type=int, default=10)
+    ap.add_argument('--drop-steps', type=int, default=30)
     a = ap.parse_args(argv)
-    if a.small:
-        experiment_small(a.out, epochs=a.epochs)
+    rr = not a.current_relative
     if a.bar:
-        experiment_bar(a.out, nx=a.bar, train_steps=a.train_steps, eval_steps=a.eval_steps, epochs=a.epochs)
+        experiment_bar(a.out, nx=a.bar, train_seed=a.train_seed, train_steps=a.train_steps, eval_start=a.eval_start,
+                       eval_steps=a.eval_steps, epochs=a.epochs, rest_relative=rr)
+    if a.drops:
+        experiment_drops(a.out, n_train=a.drops, n_eval=a.drop_eval, steps=a.drop_steps, epochs=a.epochs, rest_relative=rr)
 
 
 if __name__ == '__main__':

@@ -76,6 +76,9 @@ int fipc_ctx_set_x0(fipc_ctx* ctx, const double* x0, void* stream);
  * that there are at most 512 runs).  The solution satisfies the same tolerance either way. */
 int fipc_ctx_set_preconditioner(fipc_ctx* ctx, int agg_rows);
 int fipc_ctx_preconditioner(fipc_ctx* ctx, int* agg_rows, int* n_coarse);
+/* In-place inverse of a dense SPD matrix on the device (n a multiple of 32, row-major; work: 1024
+ * + 64 n doubles): the blocked Gauss-Jordan used for the coarse matrix, one cooperative launch. */
+int fipc_dense_spd_inverse(int n, double* a, double* work, void* stream);
 
 /* find_constraints, NEWTON_IPC.py:337-357 (spatial hash :213-334, dedup :348-356): the seven
  * lists, sorted lexicographically and de-duplicated; counts_h [7] receives their sizes. */
