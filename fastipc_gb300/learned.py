@@ -218,10 +218,10 @@ class _Recorder:
             self.inner(sim, f)
 
 
-def collect(scene, steps, device='cuda:0', pcg_rtol=1e-6, start=0, rest_relative=True):
+def collect(scene, steps, device='cuda:0', pcg_rtol=1e-6, start=0, rest_relative=True, stride=1):
     """Run the solver (inertial start, which converges to the same steps as the plain one) for
-    ``steps`` steps; returns (X [n,64], Y [n,4]) over the free vertices of steps >= start,
-    Y = (x^{n+1} - xTilde) / h."""
+    ``steps`` steps; returns (X [n,64], Y [n,4]) over the free vertices of every stride-th step
+    from start on, Y = (x^{n+1} - xTilde) / h."""
     from .newton import NewtonIPC
     sim = NewtonIPC(scene, device=device, pcg_rtol=pcg_rtol)
     rec = _Recorder(LearnedStart(kind='inertial'), rest_relative=rest_relative)
@@ -230,7 +230,7 @@ def collect(scene, steps, device='cuda:0', pcg_rtol=1e-6, start=0, rest_relative
     Xs, Ys = [], []
     for f in range(steps):
         sim.step(f)
-        if f < start:
+        if f < start or (f - start) % stride:
             continue
         X, free, xt = rec.pending
         Y = torch.zeros((sim.nV, 4), dtype=F32, device=sim.device)
@@ -316,11 +316,11 @@ def fit(X, Y, device='cuda:0', epochs=30, log=print, seed=0, rest_relative=True)
     return model, stats
 
 
-def collect_bar(nx, seed, steps, device='cuda:0', rest_relative=True, pcg_rtol=1e-6):
+def collect_bar(nx, seed, steps, device='cuda:0', rest_relative=True, pcg_rtol=1e-6, stride=1):
     """Transitions of the twisted bar (20 x 20 cross-section, nx hexes long) with the inertial start."""
     from . import scenes as S
     sc = S.twisted_bar(nx=nx, ny=20, nz=20, size=(nx / 400.0, 0.05, 0.05), seed=seed)
-    return collect(sc, steps, device, pcg_rtol, rest_relative=rest_relative)
+    return collect(sc, steps, device, pcg_rtol, rest_relative=rest_relative, stride=stride)
 
 
 def compare_starts(sim, steps, f0, modes, log=print):
@@ -353,7 +353,7 @@ def compare_starts(sim, steps, f0, modes, log=print):
 
 
 def experiment_bar(out_dir, nx=400, train_seed=1, train_steps=80, eval_seed=0, eval_start=20, eval_steps=40, device='cuda:0',
-                   epochs=15, rest_relative=True, log=print, pcg_rtol=1e-6):
+                   epochs=15, rest_relative=True, log=print, pcg_rtol=1e-6, stride=1, smooth=(0, 2, 4, 8)):
     """Train on the transitions of one twisted bar (jitter seed train_seed) and compare plain /
     inertial / learned starts on another (eval_seed), over steps [eval_start, eval_start +
     eval_steps) from one state."""
@@ -362,8 +362,8 @@ def experiment_bar(out_dir, nx=400, train_seed=1, train_steps=80, eval_seed=0, e
     from .newton import NewtonIPC
     os.makedirs(out_dir, exist_ok=True)
     t0 = time.perf_counter()
-    X, Y = collect_bar(nx, train_seed, train_steps, device, rest_relative, pcg_rtol)
-    res = {'nx': nx, 'train_seed': train_seed, 'train_steps': train_steps, 'eval_seed': eval_seed, 'eval_start': eval_start,
+    X, Y = collect_bar(nx, train_seed, train_steps, device, rest_relative, pcg_rtol, stride)
+    res = {'nx': nx, 'train_seed': train_seed, 'train_steps': train_steps, 'stride': stride, 'eval_seed': eval_seed, 'eval_start': eval_start,
            'eval_steps': eval_steps, 'rest_relative': rest_relative, 'collect_s': time.perf_counter() - t0}
     model, stats = fit(X, Y, device, epochs, log, rest_relative=rest_relative)
     del X, Y
@@ -376,7 +376,7 @@ def experiment_bar(out_dir, nx=400, train_seed=1, train_steps=80, eval_seed=0, e
     for f in range(eval_start):
         sim.step(f)
     modes = {'plain': None, 'inertial': LearnedStart(kind='inertial')}
-    for k in (0, 2, 4, 8):
+    for k in smooth:
         modes[f'mlp_s{k}'] = LearnedStart(model, kind='mlp', smooth=k)
     res['eval'] = compare_starts(sim, eval_steps, eval_start, modes, log)
     sim.close()
@@ -430,6 +430,8 @@ def main(argv=None):
     ap.add_argument('--bar', type=int, default=0, help='twisted bar with nx hexes along its axis (0: skip)')
     ap.add_argument('--train-seed', type=int, default=1)
     ap.add_argument('--train-steps', type=int, default=80)
+    ap.add_argument('--stride', type=int, default=1, help='keep every stride-th training step')
+    ap.add_argument('--smooth', default='0,2,4,8', help='smoothing passes to evaluate')
     ap.add_argument('--eval-start', type=int, default=20)
     ap.add_argument('--eval-steps', type=int, default=40)
     ap.add_argument('--current-relative', action='store_true', help='one-ring offsets x_j - x_i instead of rest-relative')
@@ -440,7 +442,8 @@ def main(argv=None):
     rr = not a.current_relative
     if a.bar:
         experiment_bar(a.out, nx=a.bar, train_seed=a.train_seed, train_steps=a.train_steps, eval_start=a.eval_start,
-                       eval_steps=a.eval_steps, epochs=a.epochs, rest_relative=rr)
+                       eval_steps=a.eval_steps, epochs=a.epochs, rest_relative=rr, stride=a.stride,
+                       smooth=tuple(int(k) for k in a.smooth.split(',')))
     if a.drops:
         experiment_drops(a.out, n_train=a.drops, n_eval=a.drop_eval, steps=a.drop_steps, epochs=a.epochs, rest_relative=rr)
 
