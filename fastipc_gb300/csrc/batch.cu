@@ -179,24 +179,27 @@ __device__ __forceinline__ int tile_scene_live(const BPCG& a, int t) {
 // tile sums of NV values into part[c * n_tiles + t]; true in every thread of the scene's last tile
 template <int TR, int NV>
 __device__ __forceinline__ bool tile_partials(const BPCG& a, int t, int s, const double (&v)[NV]) {
-    __shared__ double sh[NV][TR / 32];
+    // the values go through shared memory and warp c sums component c in a fixed order (fewer
+    // FP64 adds than a shuffle tree in every warp)
+    __shared__ double sv[NV][TR];
+    __shared__ double tot[NV];
     __shared__ bool last;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int c = 0; c < NV; ++c) {
-        double x = v[c];
+    for (int c = 0; c < NV; ++c) sv[c][threadIdx.x] = v[c];
+    __syncthreads();
+    for (int c = wid; c < NV; c += TR / 32) {
+        double x = sv[c][lane];
+#pragma unroll
+        for (int k = 1; k < TR / 32; ++k) x += sv[c][lane + 32 * k];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[c][wid] = x;
+        if (lane == 0) tot[c] = x;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < NV; ++c) {
-            double q = 0.0;
-            for (int k = 0; k < TR / 32; ++k) q += sh[c][k];
-            a.part[(size_t)c * a.n_tiles + t] = q;
-        }
+        for (int c = 0; c < NV; ++c) a.part[(size_t)c * a.n_tiles + t] = tot[c];
         __threadfence();
         const int ticket = atomicAdd(&a.sflag[4 * s + 2], 1);
         last = ticket == a.scene_tile0[s + 1] - a.scene_tile0[s] - 1;
