@@ -44,8 +44,9 @@ def parse():
     ap.add_argument('--profile-kernel', type=int, default=1, help='kernel timed for the roofline (1 = PCG SpMV)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--cpu-sample-pcg', type=int, default=100000)
-    ap.add_argument('--workload', default='bar', choices=['bar', 'batch'],
-                    help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context')
+    ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes'],
+                    help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context; '
+                         'lattice: 216 cubes dropped on a ground box; cubes: two 8^3-hex cubes')
     ap.add_argument('--scenes', type=int, default=512, help='scenes of the batch workload')
     ap.add_argument('--learned-steps', type=int, default=20,
                     help='steps run from the timed state with the inertial and the learned start (0: skip)')
@@ -53,16 +54,32 @@ def parse():
     return ap.parse_args()
 
 
-def make_scene(nx):
+def make_scene(args):
     from fastipc_gb300 import scenes
+    if args.workload == 'lattice':
+        return scenes.cube_lattice(m=6, n=6, seed=0)
+    if args.workload == 'cubes':
+        return scenes.two_cubes(n=8, seed=0)
+    nx = args.nx
     return scenes.twisted_bar(nx=nx, ny=20, nz=20, size=(nx / 400.0, 0.05, 0.05), seed=0)
 
 
-def workload(nx, pcg_rtol):
-    return {'workload': f'twisted bar {nx}x20x20 hexes x6 tets ({nx * 2400} tets), NH E=1e6 nu=0.45, dhat=5e-4, dt=0.01',
-            'tets': nx * 2400, 'verts': (nx + 1) * 441, 'newton_tol': '|p|inf < 1e-2 dt', 'pcg_rtol': pcg_rtol,
-            'pcg_tolerance': 'relative to |rhs| on free DOFs',
-            'l2': 'inputs larger than L2 (element Hessians alone ~0.7 GB per Newton iteration)'}
+def metric(args):
+    return {'lattice': 'steps/s (216-cube lattice drop, 280k tets)', 'cubes': 'steps/s (two cubes, 6k tets)'}.get(args.workload, METRIC)
+
+
+def workload(args):
+    common = {'newton_tol': '|p|inf < 1e-2 dt', 'pcg_rtol': args.pcg_rtol, 'pcg_tolerance': 'relative to |rhs| on free DOFs'}
+    if args.workload == 'lattice':
+        return dict(common, workload='6x6x6 lattice of 0.1 m cubes (6 hexes per side x6 tets), seed-drawn rotations and +-10% '
+                                     'jitter, dropped on a fixed 2x0.1x2 m ground box; NH E=1e5 nu=0.4, dhat=1e-3, dt=0.01',
+                    tets=279942, verts=74096)
+    if args.workload == 'cubes':
+        return dict(common, workload='two 0.1 m cubes of 8x8x8 hexes x6 tets, upper one rotated (seed 0) and moving at -1 m/s; '
+                                     'NH E=1e5 nu=0.4, dhat=1e-3, dt=0.01', tets=6144, verts=1458)
+    nx = args.nx
+    return dict(common, workload=f'twisted bar {nx}x20x20 hexes x6 tets ({nx * 2400} tets), NH E=1e6 nu=0.45, dhat=5e-4, dt=0.01',
+                tets=nx * 2400, verts=(nx + 1) * 441, l2='inputs larger than L2 (element Hessians alone ~0.7 GB per Newton iteration)')
 
 
 class ClockSampler:
@@ -170,7 +187,7 @@ def run_reference(args):
     if rank != 0:
         return
     from oracle import oracle as O
-    scene = make_scene(args.nx)
+    scene = make_scene(args)
     sim = O.OracleSim(scene, solver='bsr', pcg_rtol=args.pcg_rtol, pcg_maxit=args.cpu_sample_pcg)
     f = 0
     for _ in range(args.warmup):
@@ -184,9 +201,9 @@ def run_reference(args):
     dt = time.perf_counter() - t0
     its = sim.newton_iters[n0:]
     v = args.steps / dt
-    out = {'impl': 'reference', 'metric': METRIC, 'value': v, 'unit': 'steps/s', 'n_gpus': args.gpus, 'steps': args.steps,
+    out = {'impl': 'reference', 'metric': metric(args), 'value': v, 'unit': 'steps/s', 'n_gpus': args.gpus, 'steps': args.steps,
            'warmup': args.warmup, 'ms_per_step': 1e3 * dt / args.steps, 'higher_is_better': True, 'scaling': 'weak',
-           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload(args.nx, args.pcg_rtol),
+           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload(args),
            'ms_per_newton_iter': 1e3 * dt / max(sum(its), 1), 'newton_iters_per_step': sum(its) / len(its),
            'cpu_baseline': {'value': v, 'unit': 'steps/s', 'cores': O.lib().oracle_num_threads(), 'kind': 'port',
                             'sample': f'{args.steps} whole time steps ({args.warmup}..{args.warmup + args.steps - 1}) of the same scene'},
@@ -216,7 +233,7 @@ def main():
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
     build()
-    scene = make_scene(args.nx)
+    scene = make_scene(args)
     sim = NewtonIPC(scene, device=dev, pcg_rtol=args.pcg_rtol, pcg_warm_start=bool(args.warm_start))
 
     def barrier():
@@ -285,7 +302,7 @@ def main():
         e2e_ms = float(t.item())
     nbytes = 2 * sim.x.numel() * 8
 
-    learned = learned_leg(sim, snap, f0, args) if args.learned_steps > 0 else None
+    learned = learned_leg(sim, snap, f0, args) if args.learned_steps > 0 and args.workload == 'bar' else None
 
     if rank == 0:
         pk, src = peaks()
@@ -301,9 +318,9 @@ def main():
                 'peak_source': src, 'time_share_of_step': pt / ms if ms > 0 else None}
         if note:
             roof['traffic_note'] = note
-        out = {'metric': METRIC, 'value': value, 'unit': 'steps/s', 'n_gpus': world, 'steps': args.steps,
+        out = {'metric': metric(args), 'value': value, 'unit': 'steps/s', 'n_gpus': world, 'steps': args.steps,
                'warmup': args.warmup, 'ms_per_step': ms_max / args.steps, 'higher_is_better': True, 'scaling': 'weak',
-               'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload(args.nx, args.pcg_rtol),
+               'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload(args),
                'ms_per_newton_iter': ms_max / max(sum(newton), 1), 'newton_iters_per_step': newton_per_step,
                'pcg_iters_per_newton': pcg_per_newton, 'parallelism': 'replicas' if world > 1 else 'single',
                'e2e': {'value': world * args.steps / (e2e_ms / 1e3), 'unit': 'steps/s', 'h2d_bytes_per_step': nbytes,
