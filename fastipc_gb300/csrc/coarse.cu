@@ -237,28 +237,36 @@ static int launch_gauss_jordan(int n, double* A, double* buf, cudaStream_t s) {
     return FIPC_OK;
 }
 
-// u_i += P_i y_I = y_t + y_w x d_i on free vertices, y_I = rows 6I..6I+5 of Ac^-1 times g: each
-// block (one aggregate) forms its own six values, so the correction is one launch
-__global__ void __launch_bounds__(PCG_THREADS) k_cs_prolong(PCGArgs a) {
-    __shared__ double y[6];
+// y = Ac^-1 g: g (the aggregate restrictions, complete once the last PCG kernel ran) is staged in
+// shared memory, then one warp per row, fixed-order lane sums and shuffle tree
+constexpr int CS_MV_THREADS = 256;
+__global__ void __launch_bounds__(CS_MV_THREADS) k_cs_coarse(PCGArgs a) {
+    extern __shared__ double g[];
     if (*(volatile int*)&a.flag[0]) return;
-    const int I = blockIdx.x / a.cs_blocks;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int k = wid; k < 6; k += PCG_THREADS / 32) {
-        const double* Ar = a.cs_ainv + (size_t)(6 * I + k) * a.cs_ld;
+    for (int q = threadIdx.x; q < a.cs_n; q += CS_MV_THREADS) g[q] = a.cs_g[q];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warps = CS_MV_THREADS / 32;
+    for (int row = blockIdx.x * warps + (threadIdx.x >> 5); row < a.cs_n; row += gridDim.x * warps) {
+        const double* Ar = a.cs_ainv + (size_t)row * a.cs_ld;
         double t = 0.0;
-        for (int j = lane; j < a.cs_n; j += 32) t += __ldg(Ar + j) * __ldg(a.cs_g + j);
+        for (int j = lane; j < a.cs_n; j += 32) t += __ldg(Ar + j) * g[j];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
-        if (lane == 0) y[k] = t;
+        if (lane == 0) a.cs_y[row] = t;
     }
-    __syncthreads();
+}
+
+// u_i += P_i y_I = y_t + y_w x d_i on free vertices
+__global__ void __launch_bounds__(PCG_THREADS) k_cs_prolong(PCGArgs a) {
+    if (*(volatile int*)&a.flag[0]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nV || a.fixed[i]) return;
+    const double* y = a.cs_y + 6 * (size_t)(blockIdx.x / a.cs_blocks);
     const double dx = __ldg(a.cs_d + 3 * (size_t)i), dy = __ldg(a.cs_d + 3 * (size_t)i + 1), dz = __ldg(a.cs_d + 3 * (size_t)i + 2);
-    a.u[4 * (size_t)i] += y[0] + (y[4] * dz - y[5] * dy);
-    a.u[4 * (size_t)i + 1] += y[1] + (y[5] * dx - y[3] * dz);
-    a.u[4 * (size_t)i + 2] += y[2] + (y[3] * dy - y[4] * dx);
+    const double y0 = y[0], y1 = y[1], y2 = y[2], y3 = y[3], y4 = y[4], y5 = y[5];
+    a.u[4 * (size_t)i] += y0 + (y4 * dz - y5 * dy);
+    a.u[4 * (size_t)i + 1] += y1 + (y5 * dx - y3 * dz);
+    a.u[4 * (size_t)i + 2] += y2 + (y3 * dy - y4 * dx);
 }
 
 // ---------------------------------------------------------------- host side
@@ -310,7 +318,7 @@ int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
     const int n = 6 * c->cs_n_agg, nb = nblk_c(c->nV, PCG_THREADS);
     const int ld = ((n + GJ_B - 1) / GJ_B) * GJ_B;   // padded with identity rows to whole GJ blocks
     if (c->cs_Ac.ensure(8ll * ld * ld) || c->cs_buf.ensure(8ll * (GJ_B * GJ_B + 2ll * ld * GJ_B)) || c->cs_part.ensure(48ll * nb) ||
-        c->cs_gbuf.ensure(8ll * n) || c->cs_tick.ensure(4ll * c->cs_n_agg))
+        c->cs_gbuf.ensure(16ll * n) || c->cs_tick.ensure(4ll * c->cs_n_agg))
         return FIPC_ERR_CUDA;
     FIPC_CUDA(cudaMemsetAsync(c->cs_tick.p, 0, 4ll * c->cs_n_agg, s));   // aggregate tickets
     double* Ac = c->cs_Ac.as<double>();
@@ -326,6 +334,7 @@ int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
     a.cs_d = c->cs_d.as<double>();
     a.cs_part = c->cs_part.as<double>();
     a.cs_g = c->cs_gbuf.as<double>();
+    a.cs_y = a.cs_g + n;
     a.cs_ticket = c->cs_tick.as<int>();
     a.cs_ainv = Ac;
     a.cs_n = n;
@@ -336,6 +345,8 @@ int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
 
 // the coarse correction u += P Ac^-1 P^T r for the aggregate restrictions the last PCG kernel wrote
 void cs_apply(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s) {
+    k_cs_coarse<<<nblk_c(a.cs_n, CS_MV_THREADS / 32), CS_MV_THREADS, 8 * (size_t)a.cs_n, s>>>(a);
+    FIPC_LAUNCHED();
     k_cs_prolong<<<nblk_c(c->nV, PCG_THREADS), PCG_THREADS, 0, s>>>(a);
     FIPC_LAUNCHED();
 }

@@ -23,6 +23,7 @@ struct PCGArgs {
     const double* cs_d;              // [V][3] vertex offset from its aggregate's centroid
     double* cs_part;                 // [nblk][6] per-block restriction (force, torque) of r
     double* cs_g;                    // [6 n_agg] restriction per aggregate
+    double* cs_y;                    // [6 n_agg] coarse correction Ac^-1 g
     int* cs_ticket;                  // [n_agg] blocks of the aggregate done (reset by its last block)
     const double* cs_ainv;           // inverse coarse matrix, row stride cs_ld
     int cs_n, cs_ld;                 // 6 n_agg; padded row stride
