@@ -196,19 +196,33 @@ __device__ void attempt_ee(const double* __restrict__ x, const double* __restric
     if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) return;
     const v3 A0 = ld3(x, a0), A1 = ld3(x, a1), B0 = ld3(x, b0), B1 = ld3(x, b1);
     if (!ee_aabb(A0, A1, B0, B1, dh)) return;
-    const double ecn = d_EECN2(A0, A1, B0, B1);
-    const double eps = m_threshold(ld3(x0, a0), ld3(x0, a1), ld3(x0, b0), ld3(x0, b1));
-    const bool m = ecn < eps;
-    switch (ee_type(A0, A1, B0, B1)) {
-        case 0: if (d_PP(A0, B0) < dh2) { if (m) emit(s, T_PPM, a0, a1, b0, b1); else emit(s, T_PP, a0, b0, 0, 0); } break;
-        case 1: if (d_PP(A0, B1) < dh2) { if (m) emit(s, T_PPM, a0, a1, b1, b0); else emit(s, T_PP, a0, b1, 0, 0); } break;
-        case 2: if (d_PE(A0, B0, B1) < dh2) { if (m) emit(s, T_PEM, a0, a1, b0, b1); else emit(s, T_PE, a0, b0, b1, 0); } break;
-        case 3: if (d_PP(A1, B0) < dh2) { if (m) emit(s, T_PPM, a1, a0, b0, b1); else emit(s, T_PP, a1, b0, 0, 0); } break;
-        case 4: if (d_PP(A1, B1) < dh2) { if (m) emit(s, T_PPM, a1, a0, b1, b0); else emit(s, T_PP, a1, b1, 0, 0); } break;
-        case 5: if (d_PE(A1, B0, B1) < dh2) { if (m) emit(s, T_PEM, a1, a0, b0, b1); else emit(s, T_PE, a1, b0, b1, 0); } break;
-        case 6: if (d_PE(B0, A0, A1) < dh2) { if (m) emit(s, T_PEM, b0, b1, a0, a1); else emit(s, T_PE, b0, a0, a1, 0); } break;
-        case 7: if (d_PE(B1, A0, A1) < dh2) { if (m) emit(s, T_PEM, b1, b0, a0, a1); else emit(s, T_PE, b1, a0, a1, 0); } break;
-        default: if (d_EE(A0, A1, B0, B1) < dh2) { if (m) emit(s, T_EEM, a0, a1, b0, b1); else emit(s, T_EE, a0, a1, b0, b1); } break;
+    // feature pair and its distance first; the mollifier switch (EECN2 < eps_x on the rest
+    // shape) is needed only for pairs within d-hat, which is what gets emitted
+    int t;
+    double d2;
+    switch (t = ee_type(A0, A1, B0, B1)) {
+        case 0: d2 = d_PP(A0, B0); break;
+        case 1: d2 = d_PP(A0, B1); break;
+        case 2: d2 = d_PE(A0, B0, B1); break;
+        case 3: d2 = d_PP(A1, B0); break;
+        case 4: d2 = d_PP(A1, B1); break;
+        case 5: d2 = d_PE(A1, B0, B1); break;
+        case 6: d2 = d_PE(B0, A0, A1); break;
+        case 7: d2 = d_PE(B1, A0, A1); break;
+        default: d2 = d_EE(A0, A1, B0, B1); break;
+    }
+    if (!(d2 < dh2)) return;
+    const bool m = d_EECN2(A0, A1, B0, B1) < m_threshold(ld3(x0, a0), ld3(x0, a1), ld3(x0, b0), ld3(x0, b1));
+    switch (t) {
+        case 0: if (m) emit(s, T_PPM, a0, a1, b0, b1); else emit(s, T_PP, a0, b0, 0, 0); break;
+        case 1: if (m) emit(s, T_PPM, a0, a1, b1, b0); else emit(s, T_PP, a0, b1, 0, 0); break;
+        case 2: if (m) emit(s, T_PEM, a0, a1, b0, b1); else emit(s, T_PE, a0, b0, b1, 0); break;
+        case 3: if (m) emit(s, T_PPM, a1, a0, b0, b1); else emit(s, T_PP, a1, b0, 0, 0); break;
+        case 4: if (m) emit(s, T_PPM, a1, a0, b1, b0); else emit(s, T_PP, a1, b1, 0, 0); break;
+        case 5: if (m) emit(s, T_PEM, a1, a0, b0, b1); else emit(s, T_PE, a1, b0, b1, 0); break;
+        case 6: if (m) emit(s, T_PEM, b0, b1, a0, a1); else emit(s, T_PE, b0, a0, a1, 0); break;
+        case 7: if (m) emit(s, T_PEM, b1, b0, a0, a1); else emit(s, T_PE, b1, a0, a1, 0); break;
+        default: if (m) emit(s, T_EEM, a0, a1, b0, b1); else emit(s, T_EE, a0, a1, b0, b1); break;
     }
 }
 
