@@ -642,7 +642,7 @@ void free_batch(fipc_ctx* c) {
     drop_graph(c);
     if (c->cap_stream) cudaStreamDestroy((cudaStream_t)c->cap_stream);
     c->cap_stream = nullptr;
-    void* ptrs[] = {c->v_scene, c->voff_d, c->toff_d, c->s_kappa, c->s_inv_dx};
+    void* ptrs[] = {c->v_scene, c->voff_d, c->toff_d, c->s_kappa, c->s_inv_dx, c->s_hash_inv_dx};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     DBuf* bufs[] = {&c->tile_scene, &c->tile_row0, &c->scene_tile0, &c->bpcg_vec, &c->bpcg_sc, &c->bpcg_part, &c->bpcg_flag, &c->s_red,
@@ -661,6 +661,7 @@ extern "C" int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const in
 extern "C" int fipc_ctx_destroy(fipc_ctx* c);
 namespace fipc {
 int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h);
+double median_edge_inv(const double* x, const int* be, int e0, int e1, double fallback);
 }
 
 namespace {
@@ -723,7 +724,7 @@ int fipc_batch_create(fipc_ctx** out, int n_scenes, const int* vert_off, const i
     if (st) return st;
     cs_setup(c, 0, nullptr, nullptr);   // the batched PCG preconditions with block-Jacobi
     // per-scene kappa (NEWTON_IPC.py:116-124, x10 at :943) and hash cell (:127-134)
-    std::vector<double> mass(n_verts), kap(S), idx(S);
+    std::vector<double> mass(n_verts), kap(S), idx(S), hidx(S);
     if (cudaMemcpy(mass.data(), c->mass, 8ll * n_verts, cudaMemcpyDeviceToHost) != cudaSuccess) {
         fipc_ctx_destroy(c);
         return FIPC_ERR_CUDA;
@@ -742,6 +743,7 @@ int fipc_batch_create(fipc_ctx** out, int n_scenes, const int* vert_off, const i
         }
         const int ne = be_off[q + 1] - be_off[q];
         idx[q] = ne ? 1.0 / (len / (double)ne) : 1.0;
+        hidx[q] = median_edge_inv(x_rest, be, be_off[q], be_off[q + 1], idx[q]);
     }
     c->n_scenes = S;
     c->h_voff.assign(vert_off, vert_off + S + 1);
@@ -750,7 +752,8 @@ int fipc_batch_create(fipc_ctx** out, int n_scenes, const int* vert_off, const i
     c->h_inv_dx = idx;
     if (c->prim_off) cudaFree(c->prim_off);
     st = upload_vec(&c->v_scene, vs) | upload_vec(&c->voff_d, c->h_voff) | upload_vec(&c->toff_d, c->h_toff) |
-         upload_vec(&c->s_kappa, kap) | upload_vec(&c->s_inv_dx, idx) | upload_vec(&c->prim_off, poff);
+         upload_vec(&c->s_kappa, kap) | upload_vec(&c->s_inv_dx, idx) | upload_vec(&c->s_hash_inv_dx, hidx) |
+         upload_vec(&c->prim_off, poff);
     if (st) {
         fipc_ctx_destroy(c);
         return FIPC_ERR_CUDA;

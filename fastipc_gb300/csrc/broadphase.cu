@@ -601,8 +601,8 @@ static int cub_call(fipc_ctx* c, F&& f) {
 static SceneGeo geo(const fipc_ctx* c) {
     SceneGeo g;
     g.vscene = c->n_scenes > 1 ? c->v_scene : nullptr;
-    g.inv_dx_s = c->s_inv_dx;
-    g.inv_dx = c->inv_dx;
+    g.inv_dx_s = c->s_hash_inv_dx;
+    g.inv_dx = c->hash_inv_dx;
     return g;
 }
 

@@ -27,6 +27,19 @@ int launch_absmax(int n, const double* p, double* part, double* out, cudaStream_
 void free_batch(fipc_ctx* c);
 int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h);
 void cs_free(fipc_ctx* c);
+// 1 / median length of boundary edges [e0, e1) (fallback when there are none)
+double median_edge_inv(const double* x, const int* be, int e0, int e1, double fallback) {
+    if (e1 <= e0) return fallback;
+    std::vector<double> len(e1 - e0);
+    for (int i = e0; i < e1; ++i) {
+        const int a = be[2 * i], b = be[2 * i + 1];
+        const double dx = x[3 * a] - x[3 * b], dy = x[3 * a + 1] - x[3 * b + 1], dz = x[3 * a + 2] - x[3 * b + 2];
+        len[i - e0] = std::sqrt(dx * dx + dy * dy + dz * dz);
+    }
+    std::nth_element(len.begin(), len.begin() + len.size() / 2, len.end());
+    const double m = len[len.size() / 2];
+    return m > 0 ? 1.0 / m : fallback;
+}
 // default aggregate size of the two-level preconditioner: 2048 vertices, larger when needed to
 // keep the dense coarse matrix at most 6 x 512 square
 int default_agg_rows(int n_verts) {
@@ -141,6 +154,7 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
             len += std::sqrt(dx * dx + dy * dy + dz * dz);
         }
         c->inv_dx = n_be ? 1.0 / (len / (double)n_be) : 1.0;
+        c->hash_inv_dx = median_edge_inv(x_rest, be, 0, n_be, c->inv_dx);
     }
     // static block pattern: all (tet[v], tet[w]) pairs plus every diagonal
     std::vector<unsigned long long> pairs;

@@ -64,6 +64,10 @@ struct fipc_ctx_impl {
     int *tets = nullptr, *bp = nullptr, *be = nullptr, *bt = nullptr;
     double *dminv = nullptr, *vol = nullptr, *lam = nullptr, *mu = nullptr, *mass = nullptr, *x0 = nullptr;
     double dhat2 = 0, dhat = 0, kappa = 0, inv_dx = 0, dt = 0;
+    // cell size of the spatial hash: the median boundary edge.  The reference's cell is the mean
+    // (inv_dx above, kept for callers); the lists found do not depend on it, but a few long
+    // edges (a ground plane) inflate the mean until one cell holds a whole body.
+    double hash_inv_dx = 0;
     // static elastic + inertia BSR pattern (full, both triangles)
     int nnzb = 0, n_upper = 0;
     int *row_ptr = nullptr, *col_idx = nullptr;
@@ -106,7 +110,7 @@ struct fipc_ctx_impl {
     // [toff[s], toff[s+1]); its own kappa and hash cell; null tables for a single scene
     int n_scenes = 1;
     int *v_scene = nullptr, *voff_d = nullptr, *toff_d = nullptr;
-    double *s_kappa = nullptr, *s_inv_dx = nullptr;
+    double *s_kappa = nullptr, *s_inv_dx = nullptr, *s_hash_inv_dx = nullptr;
     std::vector<int> h_voff, h_toff;
     // boundary lists of scene s: points [prim_off[0][s], prim_off[0][s+1]), edges [1], triangles
     // [2] (device, 3 x (n_scenes + 1)); big-primitive flags and lists of the spatial hash
