@@ -2,12 +2,13 @@
 // (NEWTON_IPC.py:181-357), the CCD step filter (NEWTON_IPC.py:377-468) and the
 // intersection check (NEWTON_IPC.py:855-886).
 //
-// The grid has the reference's cell size (1 / inv_dx, the mean boundary edge) and the same
-// box conventions: what the reference appends to its sparse grid becomes (cell key, id)
-// pairs, radix-sorted by key; unique keys and run starts give each cell's id range, found by
-// binary search.  A candidate pair whose two cell ranges overlap in several cells is examined
-// only in the overlap's lowest cell (componentwise max of the two lower corners), so every
-// pair is tested once without a hash set.  The narrow phase applies the reference's exact
+// The grid keeps the reference's box conventions, with the median boundary edge as its cell.
+// The reference uses the mean; enumeration is complete for any cell size, so the lists are the
+// same.  What the reference appends to its sparse grid becomes (cell key, id) pairs,
+// radix-sorted by key; unique keys and run starts give each cell's id range, found through an
+// open-addressing table.  A candidate pair whose two cell ranges overlap in several cells is
+// examined only in the overlap's lowest cell (componentwise max of the two lower corners), so
+// every pair is tested once without a hash set.  The narrow phase applies the reference's exact
 // predicates; constraint rows are then sorted lexicographically and de-duplicated per list
 // exactly like np.unique(axis=0) (NEWTON_IPC.py:348-356).
 #include <cub/cub.cuh>

@@ -60,7 +60,8 @@ int fipc_compute_v(int n_verts, const double* x, const double* xn, double dt, do
 /* ---- scene context: the module state of NEWTON_IPC.py -------------------------------------- */
 
 /* Host inputs.  Computes rest shapes, volumes and lumped mass (NEWTON_IPC.py:485-494), the
- * adaptive kappa x10 (:116-124, :943), the hash cell 1/mean boundary edge (:127-134, :944)
+ * adaptive kappa x10 (:116-124, :943), inv_dx = 1/mean boundary edge (:127-134, :944; the hash
+ * itself uses the median edge, which finds the same lists)
  * and the static block pattern.  x_rest is also the mollifier rest shape (save_x0, :780-783). */
 int fipc_ctx_create(fipc_ctx** ctx, int n_verts, int n_tets, const int* tets_h, const double* x_rest_h,
                     const double* lam_h, const double* mu_h, double rho, int n_bp, const int* bp_h, int n_be,
