@@ -9,10 +9,11 @@
 // iteration; the coarse space removes them.
 //
 // Aggregates are runs of cs_agg_rows vertices, a multiple of the PCG block, so each PCG block
-// restricts its residuals into its own aggregate with one fixed-order block sum.  Ac is built
-// from the elastic + inertia blocks (one CTA per coupled aggregate pair, fixed-order sums),
-// inverted densely in place by Gauss-Jordan in one cooperative launch, and applied as a dense
-// matrix-vector product per PCG iteration.
+// restricts its residuals into its own aggregate with one fixed-order block sum, and the
+// aggregate's last block (atomic ticket) totals them.  Ac is built from the elastic + inertia
+// blocks (one CTA per coupled aggregate pair, fixed-order sums), inverted densely in place by
+// blocked Gauss-Jordan in one cooperative launch, and applied per PCG iteration as one dense
+// matrix-vector kernel followed by the prolongation.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
