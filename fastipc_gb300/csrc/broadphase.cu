@@ -163,6 +163,11 @@ __global__ void k_hash_insert(const unsigned long long* __restrict__ ukeys, cons
     }
 }
 
+// lanes per query of the edge-edge, CCD and intersection queries: a few lanes share each cell's
+// candidates (one thread per query leaves most lanes idle in the FP64 narrow phase; a whole
+// warp repeats the cell walk in every lane while most cells hold a handful of candidates)
+constexpr int QG = 8;
+
 // ---------------------------------------------------------------- constraint rows
 struct RowSink {
     int4* rows[N_TYPES];
@@ -259,8 +264,8 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
 __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
                                                  const double* __restrict__ x0, double dh, double dh2, SceneGeo g,
                                                  GridView gv, RowSink sink) {
-    // one warp per query edge; its lanes share the candidates of each cell
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    // QG lanes per query edge share the candidates of each cell
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
     if (i >= nbe) return;
     if (g.big_edge && g.big_edge[i]) return;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
@@ -274,7 +279,7 @@ __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict_
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
                 const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += 32) {
+                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
                     const int j = gv.ids[k];
                     if (!(i < j)) continue;
                     const int b0 = be[2 * j], b1 = be[2 * j + 1];
@@ -330,8 +335,8 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
 __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
                                                 const double* __restrict__ p, double dh, SceneGeo g, double eta,
                                                 GridView gv, unsigned long long* __restrict__ alpha) {
-    // one warp per query edge; its lanes share the candidates of each cell
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    // QG lanes per query edge share the candidates of each cell
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
     if (i >= nbe) return;
     if (g.big_edge && g.big_edge[i]) return;
     const int a0 = be[2 * i], a1 = be[2 * i + 1];
@@ -346,7 +351,7 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
                 const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += 32) {
+                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
                     const int j = gv.ids[k];
                     if (!(i < j)) continue;
                     const int b0 = be[2 * j], b1 = be[2 * j + 1];
@@ -378,8 +383,8 @@ __global__ void __launch_bounds__(128) k_ccd_inversion(int nT, const int4* __res
 __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restrict__ bt, const int* __restrict__ be,
                                                    const double* __restrict__ x, double dh, SceneGeo g,
                                                    GridView gv, int* __restrict__ hit) {
-    // one warp per query triangle; its lanes share the candidates of each cell
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    // QG lanes per query triangle share the candidates of each cell
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
     if (i >= nbt) return;
     if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
@@ -395,7 +400,7 @@ __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restric
                 if (*(volatile int*)hit) return;
                 const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += 32) {
+                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
                     const int j = gv.ids[k];
                     const int a0 = be[2 * j], a1 = be[2 * j + 1];
                     if (a0 == t0 || a0 == t1 || a0 == t2 || a1 == t0 || a1 == t1 || a1 == t2) continue;
@@ -796,7 +801,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         st = build_grid(c, c->ge, 1, c->nBE, c->be, x, nullptr, sg, s);
         if (st) return st;
         if (c->ge.n_entries > 0) {
-            k_find_ee<<<nblk(32ll * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, sg,
+            k_find_ee<<<nblk((long long)QG * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, sg,
                                                          view(c->ge), sink);
             FIPC_LAUNCHED();
         }
@@ -840,7 +845,7 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     st = build_grid(c, c->ge, 3, c->nBE, c->be, x, p, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0) {
-        k_ccd_ee<<<nblk(32ll * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, view(c->ge), slot);
+        k_ccd_ee<<<nblk((long long)QG * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, view(c->ge), slot);
         FIPC_LAUNCHED();
     }
     if (c->nBE > 1) {
@@ -878,7 +883,7 @@ int collision_launch(fipc_ctx* c, const double* x, int* hit, cudaStream_t s) {
     st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0 && c->nBT > 0) {
-        k_collision<<<nblk(32ll * c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, sg, view(c->ge), hit);
+        k_collision<<<nblk((long long)QG * c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, sg, view(c->ge), hit);
         FIPC_LAUNCHED();
     }
     if (c->nBT > 0 && c->nBE > 0) {
