@@ -1,5 +1,4 @@
-// Newton system: assembly into 3x3 block-sparse rows and the block-Jacobi PCG direction
-// solve.  Replaces the triplet assembly of NEWTON_IPC.py:545-747 and the CHOLMOD solve of
+// Newton system: assembly into 3x3 block-sparse rows and the PCG direction solve.  Replaces the triplet assembly of NEWTON_IPC.py:545-747 and the CHOLMOD solve of
 // NEWTON_IPC.py:750-777.
 //
 // Assembly has no order-dependent atomics.  The elastic+inertia pattern is static: each
@@ -10,10 +9,11 @@
 // each run is summed by one thread into a second block-sparse matrix.  The same runs on the
 // diagonal carry the constraint gradients into the right-hand side.
 //
-// PCG: block-Jacobi preconditioner (inverse 3x3 diagonal blocks), Dirichlet vertices removed
-// by zero rows/columns (the reference's DBC_set_zeros + identity, NEWTON_IPC.py:756-772).
-// Two kernels per iteration on a fixed grid; dot products are per-block partials summed in a
-// fixed order by every consumer block, so results are bitwise reproducible.
+// PCG: block-Jacobi preconditioner (inverse 3x3 diagonal blocks) plus, by default, the
+// rigid-body coarse correction of coarse.cu; Dirichlet vertices removed by zero rows/columns
+// (the reference's DBC_set_zeros + identity, NEWTON_IPC.py:756-772).  Per iteration an SpMV and
+// an update kernel on a fixed grid (plus the two coarse kernels); dot products are per-block
+// partials summed in a fixed order by the last block, so results are bitwise reproducible.
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
