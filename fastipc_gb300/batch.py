@@ -93,6 +93,12 @@ class BatchNewtonIPC:
         self.iters = torch.zeros(S, dtype=torch.int32, device=dev)
         self.active_d = torch.ones(S, dtype=torch.uint8, device=dev)
         self.counts = [0] * 7
+        # scene of every vertex (device), for per-scene selections on the host side
+        self.v_scene = torch.repeat_interleave(torch.arange(S, device=dev), torch.from_numpy(np.diff(self.voff).astype(np.int64)).to(dev))
+        # optional Newton initial guess hook, called as initial_guess(sim, f) after move_nodes;
+        # dx_prev: the displacement of the step before the last one (for such hooks)
+        self.initial_guess = None
+        self.dx_prev = torch.zeros_like(self.x)
         self.newton_iters = []     # per step: numpy [S]
         self.pcg_iters = []        # per solve: numpy [S]
 
@@ -220,6 +226,8 @@ class BatchNewtonIPC:
         with self.timer('Time Step'):
             self.compute_xn_and_xTilde()
             self.move_nodes(f * self.dt)
+            if self.initial_guess is not None:
+                self.initial_guess(self, f)
             active = np.ones(S, bool)
             its = np.zeros(S, np.int64)
             while True:
@@ -269,6 +277,7 @@ class BatchNewtonIPC:
                         k += 1
                         if k > self.max_halvings:
                             raise FastIPCError(2, 'line search: collision halving limit')
+            torch.mul(self.v, self.dt, out=self.dx_prev)
             self.compute_v()
         self.newton_iters.append(its)
         return its

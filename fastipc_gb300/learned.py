@@ -37,6 +37,10 @@ def _p(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
+def _log(msg):
+    print(msg, flush=True)
+
+
 class WarmStartMLP:
     IN, H, OUT = 64, 128, 4
 
@@ -203,6 +207,77 @@ class LearnedStart:
 
 
 # ---------------------------------------------------------------------- data and training
+class BatchLearnedStart:
+    """``BatchNewtonIPC.initial_guess`` hook: for every scene of a batch, the lowest-energy
+    filtered start among x^n, the inertial step and (kind 'mlp') the learned step, exactly as
+    ``LearnedStart`` chooses for one scene.  Every scene gets its own CCD step, collision halving
+    and choice.  The network's inputs are divided by one cell size, so the scenes of the batch
+    must share it (same mesh resolution)."""
+
+    def __init__(self, model=None, kind='mlp', smooth=4, max_halvings=64):
+        assert kind in ('mlp', 'inertial')
+        assert kind == 'inertial' or model is not None
+        self.model, self.kind, self.smooth, self.max_halvings = model, kind, smooth, max_halvings
+        self.chosen = {'plain': 0, 'inertial': 0, 'mlp': 0}
+        self._X = self._tmp = None
+
+    def _learned(self, sim, d0, free):
+        if not np.allclose(sim.inv_dx, sim.inv_dx[0], rtol=1e-12):
+            raise ValueError('the learned start needs scenes with one cell size')
+        if self._X is None or self._X.shape[0] != sim.nV:
+            self._X = torch.empty((sim.nV, WarmStartMLP.IN), dtype=F32, device=sim.device)
+            self._tmp = torch.empty((sim.nV, 3), dtype=torch.float64, device=sim.device)
+        h = 1.0 / float(sim.inv_dx[0])
+        check(N.lib().fipc_mlp_features(sim.ctx, N.dptr(sim.x, torch.float64), N.dptr(sim.v, torch.float64),
+                                        N.dptr(sim.dx_prev, torch.float64), ctypes.c_double(h), int(self.model.rest_relative),
+                                        _p(self._X), N.stream()), 'mlp_features')
+        out = self.model.forward(self._X)
+        corr = torch.where(free, out[:, :3].to(torch.float64) * (self.model.scale * h), torch.zeros_like(d0)).contiguous()
+        if self.smooth:
+            check(N.lib().fipc_mlp_smooth(sim.ctx, N.dptr(sim.fixed, torch.uint8), N.dptr(corr, torch.float64),
+                                          N.dptr(self._tmp, torch.float64), int(self.smooth), N.stream()), 'mlp_smooth')
+        return d0 + corr
+
+    def __call__(self, sim, f):
+        sim.find_constraints()
+        e_best = sim.compute_energy(torch.empty_like(sim.E)).clone()
+        choice = torch.zeros(sim.S, dtype=torch.int64, device=sim.device)
+        a_best = torch.zeros_like(sim.alpha)
+        sim.save_xPrev()
+        free = (sim.fixed == 0).unsqueeze(1)
+        d0 = torch.where(free, sim.xTilde - sim.x, torch.zeros_like(sim.x))
+        cands = [d0]
+        if self.kind == 'mlp':
+            cands.append(self._learned(sim, d0, free))   # features at x^n (lists found above)
+        for idx, d in enumerate(cands, start=1):
+            sim.data_sol.copy_(d)
+            sim.compute_intersection_free_step_size()
+            sim.apply_sol()
+            valid = np.ones(sim.S, bool)
+            for _ in range(self.max_halvings + 1):
+                hit = sim.check_collision()
+                if not hit.any():
+                    break
+                sim._halve(hit)
+            valid &= ~sim.check_collision()
+            sim.find_constraints()
+            e = sim.compute_energy()
+            better = torch.from_numpy(valid).to(sim.device) & (e < e_best)
+            e_best = torch.where(better, e, e_best)
+            choice = torch.where(better, torch.full_like(choice, idx), choice)
+            a_best = torch.where(better, sim.alpha, a_best)
+        cv = choice[sim.v_scene].unsqueeze(1)
+        d = torch.zeros_like(sim.x)
+        for idx, c in enumerate(cands, start=1):
+            d = torch.where(cv == idx, c, d)
+        sim.data_sol.copy_(d)
+        sim.alpha.copy_(a_best)
+        sim.apply_sol()
+        counts = torch.bincount(choice, minlength=3).cpu().numpy()
+        for k, name in enumerate(('plain', 'inertial', 'mlp')):
+            self.chosen[name] += int(counts[k])
+
+
 class _Recorder:
     """Hook that records (features, free mask, inertial predictor) at each step's start."""
 
@@ -301,7 +376,7 @@ def _split(X, Y, seed=0):
     return X[perm[nval:]].contiguous(), Y[perm[nval:]].contiguous(), X[perm[:nval]].contiguous(), Y[perm[:nval]].contiguous()
 
 
-def fit(X, Y, device='cuda:0', epochs=30, log=print, seed=0, rest_relative=True):
+def fit(X, Y, device='cuda:0', epochs=30, log=_log, seed=0, rest_relative=True):
     """Train a model on (X, Y in h units); the target scale is the RMS of Y.  Returns the model
     and its statistics (validation MSE of the network and of the inertial guess, in h^2)."""
     Xt, Yt, Xv, Yv = _split(X, Y, seed)
@@ -323,7 +398,7 @@ def collect_bar(nx, seed, steps, device='cuda:0', rest_relative=True, pcg_rtol=1
     return collect(sc, steps, device, pcg_rtol, rest_relative=rest_relative, stride=stride)
 
 
-def compare_starts(sim, steps, f0, modes, log=print):
+def compare_starts(sim, steps, f0, modes, log=_log):
     """Run steps [f0, f0 + steps) from sim's current state once per mode (the state is restored
     between modes).  modes: name -> None (plain) or a LearnedStart."""
     snap = (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone())
@@ -353,7 +428,7 @@ def compare_starts(sim, steps, f0, modes, log=print):
 
 
 def experiment_bar(out_dir, nx=400, train_seed=1, train_steps=80, eval_seed=0, eval_start=20, eval_steps=40, device='cuda:0',
-                   epochs=15, rest_relative=True, log=print, pcg_rtol=1e-6, stride=1, smooth=(0, 2, 4, 8)):
+                   epochs=15, rest_relative=True, log=_log, pcg_rtol=1e-6, stride=1, smooth=(0, 2, 4, 8)):
     """Train on the transitions of one twisted bar (jitter seed train_seed) and compare plain /
     inertial / learned starts on another (eval_seed), over steps [eval_start, eval_start +
     eval_steps) from one state."""
@@ -386,7 +461,7 @@ def experiment_bar(out_dir, nx=400, train_seed=1, train_steps=80, eval_seed=0, e
 
 
 def experiment_drops(out_dir, n_train=40, n_eval=10, steps=30, m=2, n=4, device='cuda:0', epochs=15, rest_relative=True,
-                     smooth=4, log=print, pcg_rtol=1e-6):
+                     smooth=4, log=_log, pcg_rtol=1e-6):
     """Lattice drops in the style of the 216-cube configuration (m^3 cubes of n^3 hexes over a
     ground box): train on seeds [0, n_train), compare starts on seeds [1000, 1000 + n_eval)."""
     import os
@@ -422,6 +497,41 @@ def experiment_drops(out_dir, n_train=40, n_eval=10, steps=30, m=2, n=4, device=
     return res
 
 
+def evaluate_drops_batched(model, n_eval=20, steps=30, m=2, n=4, first_seed=1000, smooth=4, device='cuda:0', pcg_rtol=1e-6,
+                           log=_log):
+    """Plain / inertial / learned starts on n_eval unseen lattice drops stepped together in one
+    batch context (each scene keeps its own Newton loop and its own start choice)."""
+    from . import scenes as S
+    from .batch import BatchNewtonIPC
+    scs = [S.cube_lattice(m=m, n=n, seed=first_seed + k) for k in range(n_eval)]
+    sim = BatchNewtonIPC(scs, device=device, pcg_rtol=pcg_rtol)
+    x0, v0 = sim.x.clone(), sim.v.clone()
+    res = {}
+    for name, guess in (('plain', None), ('inertial', BatchLearnedStart(kind='inertial')),
+                        ('learned', BatchLearnedStart(model, kind='mlp', smooth=smooth))):
+        sim.x.copy_(x0)
+        sim.v.copy_(v0)
+        sim.dx_prev.zero_()
+        sim.newton_iters = []
+        sim.initial_guess = guess
+        inter = 0
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for f in range(steps):
+            sim.step(f)
+            inter += int(sim.check_collision().sum())
+        torch.cuda.synchronize()
+        its = np.stack(sim.newton_iters)
+        res[name] = {'newton': int(its.sum()), 'newton_per_scene_step': float(its.mean()), 'wall_s': time.perf_counter() - t0,
+                     'intersecting_scene_steps': inter, 'chosen': dict(guess.chosen) if guess else None}
+        if log:
+            log(f"{name}: newton {res[name]['newton']} ({res[name]['newton_per_scene_step']:.2f} per scene-step) "
+                f"wall {res[name]['wall_s']:.1f} s")
+    sim.close()
+    res['config'] = {'n_eval': n_eval, 'steps': steps, 'm': m, 'n': n, 'seeds': [first_seed, first_seed + n_eval - 1], 'smooth': smooth}
+    return res
+
+
 def main(argv=None):
     import argparse
     ap = argparse.ArgumentParser(description='train and evaluate the learned Newton warm start')
@@ -438,12 +548,19 @@ def main(argv=None):
     ap.add_argument('--drops', type=int, default=0, help='lattice drops: number of training seeds (0: skip)')
     ap.add_argument('--drop-eval', type=int, default=10)
     ap.add_argument('--drop-steps', type=int, default=30)
+    ap.add_argument('--drop-weights', default='', help='evaluate these weights on unseen drops (batched) instead of training')
     a = ap.parse_args(argv)
     rr = not a.current_relative
     if a.bar:
         experiment_bar(a.out, nx=a.bar, train_seed=a.train_seed, train_steps=a.train_steps, eval_start=a.eval_start,
                        eval_steps=a.eval_steps, epochs=a.epochs, rest_relative=rr, stride=a.stride,
                        smooth=tuple(int(k) for k in a.smooth.split(',')))
+    if a.drop_weights:
+        import os
+        r = evaluate_drops_batched(WarmStartMLP.load(a.drop_weights), n_eval=a.drop_eval, steps=a.drop_steps)
+        os.makedirs(a.out, exist_ok=True)
+        with open(os.path.join(a.out, 'drops_eval.json'), 'w') as fh:
+            json.dump(r, fh, indent=1)
     if a.drops:
         experiment_drops(a.out, n_train=a.drops, n_eval=a.drop_eval, steps=a.drop_steps, epochs=a.epochs, rest_relative=rr)
 

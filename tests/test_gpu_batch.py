@@ -127,3 +127,29 @@ def test_full_steps_match_single_scenes():
     batch.close()
     for s in singles:
         s.close()
+
+
+def test_batched_start_choice_matches_single_scenes():
+    """BatchLearnedStart picks, for every scene, the start that LearnedStart picks for the scene
+    alone (here the filtered inertial guess against x^n), and the steps stay intersection-free."""
+    from fastipc_gb300.learned import BatchLearnedStart, LearnedStart
+    sc = [scenes.two_cubes(n=2, seed=1), scenes.two_cubes(n=3, seed=2), scenes.cube_stack(8, max_cubes=3, max_hex=3)]
+    batch = BatchNewtonIPC(sc, pcg_rtol=1e-12)
+    hook = BatchLearnedStart(kind='inertial')
+    batch.initial_guess = hook
+    singles, hooks = [], []
+    for s in sc:
+        one = NewtonIPC(s, pcg_rtol=1e-12)
+        one.initial_guess = LearnedStart(kind='inertial')
+        singles.append(one)
+        hooks.append(one.initial_guess)
+    for f in range(3):
+        its = batch.step(f)
+        for k, one in enumerate(singles):
+            assert one.step(f) == its[k]
+        assert not batch.check_collision().any()
+    total = {name: sum(h.chosen[name] for h in hooks) for name in ('plain', 'inertial')}
+    assert {name: hook.chosen[name] for name in ('plain', 'inertial')} == total
+    batch.close()
+    for one in singles:
+        one.close()
