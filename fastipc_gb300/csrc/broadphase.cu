@@ -163,9 +163,9 @@ __global__ void k_hash_insert(const unsigned long long* __restrict__ ukeys, cons
     }
 }
 
-// lanes per grid query (constraints, CCD, intersection): a few lanes share each cell's
-// candidates.  One thread per query leaves most lanes idle in the FP64 narrow phase; a whole
-// warp repeats the cell walk in every lane while most cells hold a handful of candidates.
+// lanes per query of the edge-edge, CCD and intersection queries: a few lanes share each cell's
+// candidates (one thread per query leaves most lanes idle in the FP64 narrow phase; a whole
+// warp repeats the cell walk in every lane while most cells hold a handful of candidates)
 constexpr int QG = 8;
 
 // ---------------------------------------------------------------- constraint rows
@@ -236,8 +236,7 @@ __device__ void attempt_ee(const double* __restrict__ x, const double* __restric
 __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
                                                  const double* __restrict__ x, double dh, double dh2, SceneGeo g,
                                                  GridView gv, RowSink sink) {
-    // QG lanes per query triangle share the candidates of each cell
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
@@ -250,7 +249,7 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
                 const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
+                for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
                     const int j = gv.ids[k];
                     const int p = bp[j];
                     const C3 plo = cell_of(ld3(x, p) - mk(dh, dh, dh), inv_dx);
@@ -301,8 +300,7 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* slot, double 
 __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
                                                 const double* __restrict__ x, const double* __restrict__ p, double dh, SceneGeo g,
                                                 double eta, GridView gv, unsigned long long* __restrict__ alpha) {
-    // QG lanes per query triangle share the candidates of each cell
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     if (g.big_tri && g.big_tri[i]) return;
     const int t0 = bt[3 * i], t1 = bt[3 * i + 1], t2 = bt[3 * i + 2];
@@ -319,7 +317,7 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
                 const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
-                for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
+                for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
                     const int pp = bp[gv.ids[k]];
                     if (pp == t0 || pp == t1 || pp == t2) continue;
                     const v3 P = ld3(x, pp), dP = ld3(p, pp);
@@ -792,7 +790,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         st = build_grid(c, c->gp, 0, c->nBP, c->bp, x, nullptr, sg, s);
         if (st) return st;
         if (c->gp.n_entries > 0 && c->nBT > 0) {
-            k_find_pt<<<nblk((long long)QG * c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, sg,
+            k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, sg,
                                                          view(c->gp), sink);
             FIPC_LAUNCHED();
         }
@@ -836,7 +834,7 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     st = build_grid(c, c->gp, 2, c->nBP, c->bp, x, p, sg, s);
     if (st) return st;
     if (c->gp.n_entries > 0 && c->nBT > 0) {
-        k_ccd_pt<<<nblk((long long)QG * c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, sg, eta,
+        k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, sg, eta,
                                                     view(c->gp), slot);
         FIPC_LAUNCHED();
     }
