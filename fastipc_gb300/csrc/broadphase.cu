@@ -163,9 +163,10 @@ __global__ void k_hash_insert(const unsigned long long* __restrict__ ukeys, cons
     }
 }
 
-// lanes per query of the edge-edge, CCD and intersection queries: a few lanes share each cell's
-// candidates (one thread per query leaves most lanes idle in the FP64 narrow phase; a whole
-// warp repeats the cell walk in every lane while most cells hold a handful of candidates)
+// lanes per edge-edge constraint, edge-edge CCD and intersection query: a few lanes share each
+// cell's candidates.  One thread per query leaves most lanes idle in the FP64 narrow phase; a
+// whole warp repeats the cell walk in every lane while most cells hold a handful of candidates.
+// The point-triangle queries, whose cells hold fewer candidates, keep one thread per query.
 constexpr int QG = 8;
 
 // ---------------------------------------------------------------- constraint rows
