@@ -12,12 +12,12 @@ from .build import LIB
 _lib = None
 
 STATUS = {0: 'ok', 1: 'capacity exceeded', 2: 'iteration limit reached', 3: 'non-finite value', 4: 'CUDA error',
-          5: 'invalid argument'}
+          5: 'invalid argument', 6: 'file I/O error'}
 
 # symbols declared in include/fastipc.h
 EXPORTS = [
     'fipc_elasticity', 'fipc_barrier_rows', 'fipc_ccd_pairs', 'fipc_inversion_free_pairs', 'fipc_compute_xn_and_xtilde',
-    'fipc_move_nodes', 'fipc_apply_sol', 'fipc_compute_v', 'fipc_ctx_create', 'fipc_ctx_destroy', 'fipc_ctx_params',
+    'fipc_move_nodes', 'fipc_dirichlet_script', 'fipc_apply_sol', 'fipc_compute_v', 'fipc_ctx_create', 'fipc_ctx_destroy', 'fipc_ctx_params',
     'fipc_ctx_set_params', 'fipc_ctx_mass', 'fipc_ctx_set_x0', 'fipc_find_constraints', 'fipc_get_constraints',
     'fipc_compute_hessian_and_gradient', 'fipc_system_sizes', 'fipc_export_system', 'fipc_solve_system',
     'fipc_output_residual', 'fipc_compute_energy', 'fipc_compute_intersection_free_step_size', 'fipc_check_collision',
@@ -26,6 +26,7 @@ EXPORTS = [
     'fipc_mlp_adam', 'fipc_mlp_features', 'fipc_batch_create', 'fipc_batch_params', 'fipc_batch_compute_energy',
     'fipc_batch_output_residual', 'fipc_batch_step_size', 'fipc_batch_check_collision', 'fipc_batch_apply_sol',
     'fipc_batch_solve_system', 'fipc_batch_pcg_shape', 'fipc_ctx_set_preconditioner', 'fipc_ctx_preconditioner', 'fipc_mlp_smooth', 'fipc_dense_spd_inverse',
+    'fipc_write_obj',
 ]
 
 

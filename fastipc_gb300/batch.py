@@ -48,7 +48,7 @@ def concat_scenes(scenes):
 
 class BatchNewtonIPC:
     def __init__(self, scenes, device='cuda:0', pcg_rtol=1e-10, pcg_maxit=200000, eta=0.2, inversion_filter=True,
-                 max_newton=500, max_halvings=64):
+                 max_newton=500, max_halvings=64, device_dirichlet=True):
         if len(scenes) < 2:
             raise FastIPCError(5, 'a batch needs at least two scenes (use NewtonIPC for one)')
         first = scenes[0]
@@ -84,6 +84,20 @@ class BatchNewtonIPC:
         self.fixed = torch.zeros(self.nV, dtype=torch.uint8, device=dev)
         self.target = torch.zeros_like(self.x)
         self._dir_key = None
+        # the scenes' Dirichlet schedules on the device when every scene gives one as rigid
+        # motions of vertex groups (group ids offset per scene)
+        self._script = None
+        if device_dirichlet and all(getattr(sc, 'dirichlet_motion', None) is not None for sc in scenes):
+            grp, mot, g0 = [], [], 0
+            for sc in scenes:
+                gs = np.asarray(sc.dirichlet_groups, dtype=np.int32)
+                grp.append(np.where(gs >= 0, gs + g0, -1).astype(np.int32))
+                m = np.asarray(sc.dirichlet_motion, dtype=np.float64).reshape(-1, 10)
+                mot.append(m)
+                g0 += len(m)
+            self._script = (torch.tensor(u['x0'], dtype=F64, device=dev).contiguous(),
+                            torch.tensor(np.concatenate(grp), device=dev).contiguous(),
+                            torch.tensor(np.concatenate(mot), dtype=F64, device=dev).contiguous())
         S = self.S
         self.E0 = torch.zeros(S, dtype=F64, device=dev)
         self.E = torch.zeros(S, dtype=F64, device=dev)
@@ -122,6 +136,13 @@ class BatchNewtonIPC:
 
     def _dirichlet(self, t):
         if self._dir_key == t:
+            return
+        if self._script is not None:
+            xr, grp, mot = self._script
+            check(N.lib().fipc_dirichlet_script(self.nV, dptr(xr, F64), dptr(grp, torch.int32), len(mot), dptr(mot, F64), D(t),
+                                                dptr(self.fixed, torch.uint8), dptr(self.target, F64), self._s()),
+                  'dirichlet_script')
+            self._dir_key = t
             return
         masks, vals = zip(*(sc.dirichlet(t) for sc in self.scenes))
         self.fixed.copy_(torch.from_numpy(np.concatenate(masks).astype(np.uint8)))

@@ -39,6 +39,7 @@ enum : int {
     FIPC_ERR_NONFINITE = 3,
     FIPC_ERR_CUDA = 4,
     FIPC_ERR_ARGUMENT = 5,
+    FIPC_ERR_IO = 6,
 };
 
 // constraint lists, in the reference's order (NEWTON_IPC.py:349)

@@ -197,6 +197,41 @@ __global__ void k_move_nodes(int nV, const unsigned char* __restrict__ fixed, co
         xt[i] = target[i];
     }
 }
+// settings['dirichlet'](t) of projects/FastIPC/reader.py:154-357 evaluated on the device for
+// schedules that are rigid motions of vertex groups: group g moves its rest positions by the
+// rotation about the unit axis a through c at omega rad/s (Rodrigues' formula), then
+// translates them by u t.  motion[g] = (c[3], a[3], omega, u[3]).  Vertices with group < 0
+// are free and keep their rest position as target, as the reference's copy of the particles
+// does.  One thread per vertex.
+__global__ void k_dirichlet_script(int nV, const double* __restrict__ xr, const int* __restrict__ group, int n_groups,
+                                   const double* __restrict__ motion, double t, unsigned char* __restrict__ fixed,
+                                   double* __restrict__ target) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nV) return;
+    const int g = group[i];
+    const double px = xr[3 * (size_t)i], py = xr[3 * (size_t)i + 1], pz = xr[3 * (size_t)i + 2];
+    if (g < 0 || g >= n_groups) {
+        fixed[i] = 0;
+        target[3 * (size_t)i] = px;
+        target[3 * (size_t)i + 1] = py;
+        target[3 * (size_t)i + 2] = pz;
+        return;
+    }
+    const double* m = motion + 10 * (size_t)g;
+    const double rx = px - m[0], ry = py - m[1], rz = pz - m[2];
+    const double ax = m[3], ay = m[4], az = m[5];
+    double sn, cs;
+    sincos(m[6] * t, &sn, &cs);
+    // R r = r cos + (a x r) sin + a (a . r)(1 - cos)
+    const double ad = (ax * rx + ay * ry + az * rz) * (1.0 - cs);
+    const double qx = rx * cs + (ay * rz - az * ry) * sn + ax * ad;
+    const double qy = ry * cs + (az * rx - ax * rz) * sn + ay * ad;
+    const double qz = rz * cs + (ax * ry - ay * rx) * sn + az * ad;
+    fixed[i] = 1;
+    target[3 * (size_t)i] = m[0] + qx + m[7] * t;
+    target[3 * (size_t)i + 1] = m[1] + qy + m[8] * t;
+    target[3 * (size_t)i + 2] = m[2] + qz + m[9] * t;
+}
 // NEWTON_IPC.py:792-796
 __global__ void k_apply_sol(int n, const double* __restrict__ xprev, const double* __restrict__ sol, double alpha,
                             double* __restrict__ x) {
@@ -348,6 +383,18 @@ int fipc_move_nodes(int n_verts, const unsigned char* fixed, const double* targe
     return FIPC_OK;
 }
 
+int fipc_dirichlet_script(int n_verts, const double* x_rest, const int* group, int n_groups, const double* motion, double t,
+                          unsigned char* fixed, double* target, void* stream) {
+    if (n_verts < 0 || n_groups < 0 || !x_rest || !group || (n_groups > 0 && !motion) || !fixed || !target)
+        return FIPC_ERR_ARGUMENT;
+    if (n_verts == 0) return FIPC_OK;
+    k_dirichlet_script<<<nblk(n_verts, 256), 256, 0, (cudaStream_t)stream>>>(n_verts, x_rest, group, n_groups, motion, t, fixed,
+                                                                             target);
+    FIPC_LAUNCHED();
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+
 int fipc_apply_sol(int n_verts, const double* xprev, const double* sol, double alpha, double* x, void* stream) {
     if (n_verts < 0 || !xprev || !sol || !x) return FIPC_ERR_ARGUMENT;
     if (n_verts == 0) return FIPC_OK;
@@ -376,6 +423,7 @@ const char* fipc_status_string(int status) {
         case FIPC_ERR_NONFINITE: return "non-finite value";
         case FIPC_ERR_CUDA: return "CUDA error";
         case FIPC_ERR_ARGUMENT: return "invalid argument";
+        case FIPC_ERR_IO: return "file I/O error";
         default: return "unknown status";
     }
 }

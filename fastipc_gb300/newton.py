@@ -48,7 +48,7 @@ class Timer:
 
 class NewtonIPC:
     def __init__(self, scene, device='cuda:0', pcg_rtol=1e-10, pcg_maxit=200000, eta=0.2, inversion_filter=True,
-                 max_newton=500, max_halvings=64, pcg_warm_start=False, coarse_agg=None):
+                 max_newton=500, max_halvings=64, pcg_warm_start=False, coarse_agg=None, device_dirichlet=True):
         self.scene = scene
         self.device = torch.device(device)
         torch.cuda.set_device(self.device)
@@ -92,6 +92,13 @@ class NewtonIPC:
         self._dir_key = None
         self.fixed = torch.zeros(self.nV, dtype=torch.uint8, device=dev)
         self.target = torch.zeros_like(self.x)
+        # the Dirichlet schedule on the device (fipc_dirichlet_script) when the scene gives it as
+        # rigid motions of vertex groups; otherwise scene.dirichlet(t) runs on the host
+        self._script = None
+        if device_dirichlet and getattr(scene, 'dirichlet_motion', None) is not None:
+            self._script = (torch.tensor(rest, dtype=F64, device=dev).contiguous(),
+                            torch.tensor(np.asarray(scene.dirichlet_groups, dtype=np.int32), device=dev).contiguous(),
+                            torch.tensor(np.asarray(scene.dirichlet_motion, dtype=np.float64), device=dev).reshape(-1, 10).contiguous())
         self.newton_iters = []
         self.pcg_iters = []
         self.alphas = []
@@ -144,8 +151,15 @@ class NewtonIPC:
         return m
 
     def _dirichlet(self, t):
-        # settings['dirichlet'](t) is a function of t only: upload once per distinct t
+        # settings['dirichlet'](t) is a function of t only: evaluate once per distinct t
         if self._dir_key == t:
+            return
+        if self._script is not None:
+            xr, grp, mot = self._script
+            check(N.lib().fipc_dirichlet_script(self.nV, dptr(xr, F64), dptr(grp, torch.int32), len(mot), dptr(mot, F64), D(t),
+                                                dptr(self.fixed, torch.uint8), dptr(self.target, F64), self._s()),
+                  'dirichlet_script')
+            self._dir_key = t
             return
         mask, val = self.scene.dirichlet(t)
         self.fixed.copy_(torch.from_numpy(np.ascontiguousarray(mask.astype(np.uint8))))
@@ -257,6 +271,43 @@ class NewtonIPC:
     def compute_v(self):
         check(N.lib().fipc_compute_v(self.nV, dptr(self.x, F64), dptr(self.xn, F64), D(self.dt), dptr(self.v, F64), self._s()),
               'compute_v')
+
+    def set_state(self, x, v):
+        """Positions and velocities [V,3] (host or device), as the restart of NEWTON_IPC.py:949-953
+        loads them."""
+        self.x.copy_(torch.as_tensor(np.asarray(x, dtype=np.float64) if not isinstance(x, torch.Tensor) else x).reshape(-1, 3))
+        self.v.copy_(torch.as_tensor(np.asarray(v, dtype=np.float64) if not isinstance(v, torch.Tensor) else v).reshape(-1, 3))
+
+    # ------------------------------------------------------------------ the main loop
+    def run(self, n_frames, directory=None, start_frame=0, obj=True, cache=True):
+        """The reference's main loop (NEWTON_IPC.py:947-1003) for n_frames time steps.  With a
+        directory, frame 0 and every frame after a step go to objs/%06d.obj and
+        caches/%06d.p as the reference writes them (through ``frames.FrameWriter``, off the
+        simulation stream); start_frame > 0 restarts from caches/{start_frame:06d}.p.  Returns
+        the Newton iteration count of every step."""
+        from . import frames
+        writer = None
+        if directory is not None and (obj or cache):
+            writer = frames.FrameWriter(directory, self.scene.boundary_triangles, self.nV, obj=obj, cache=cache)
+        try:
+            if writer is not None:
+                writer.submit(0, self.x, self.v, cache=False)   # write_image(0) (NEWTON_IPC.py:947)
+            if start_frame > 0:
+                if writer is not None:
+                    writer.flush()
+                x, v = frames.load_cache(frames.cache_path(directory, start_frame))
+                self.set_state(x, v)
+            its = []
+            for f in range(start_frame, start_frame + n_frames):
+                its.append(self.step(f))
+                if writer is not None:
+                    writer.submit(f + 1, self.x, self.v)
+            if writer is not None:
+                writer.flush()
+        finally:
+            if writer is not None:
+                writer.close()
+        return its
 
     # ------------------------------------------------------------------ the time step
     def step(self, f, record=None):

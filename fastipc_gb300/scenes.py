@@ -91,6 +91,12 @@ class Scene:
     steps: int = 50
     meta: dict = field(default_factory=dict)
     x_init: np.ndarray = None     # [V,3] initial positions when they differ from the rest shape
+    # the Dirichlet schedule as rigid motions of vertex groups, evaluated on the device by
+    # fipc_dirichlet_script when present: group [V] i32 (-1 free), motion [G,10] f64 =
+    # (centre[3], unit axis[3], omega rad/s, velocity[3]); ``dirichlet`` is the same schedule
+    # written as the reference's per-vertex loop
+    dirichlet_groups: np.ndarray = None
+    dirichlet_motion: np.ndarray = None
 
     def initial_positions(self):
         return self.x if self.x_init is None else self.x_init
@@ -104,7 +110,7 @@ class Scene:
         return len(self.tets)
 
 
-def _finish(name, parts, v, dirichlet_fn, **kw):
+def _finish(name, parts, v, dirichlet_fn, script=None, **kw):
     xs, ts, off = [], [], 0
     for x, t in parts:
         xs.append(x)
@@ -113,7 +119,16 @@ def _finish(name, parts, v, dirichlet_fn, **kw):
     x = np.concatenate(xs).astype(np.float64)
     tets = np.concatenate(ts).astype(np.int32)
     bp, be, bt = find_boundary(tets)
-    return Scene(name, x, tets, v, bp, be, bt, dirichlet_fn(x), **kw)
+    groups, motion = (None, None) if script is None else script
+    return Scene(name, x, tets, v, bp, be, bt, dirichlet_fn(x), dirichlet_groups=groups, dirichlet_motion=motion, **kw)
+
+
+def motion_row(centre=(0.0, 0.0, 0.0), axis=(1.0, 0.0, 0.0), omega=0.0, velocity=(0.0, 0.0, 0.0)):
+    """One group's rigid motion for fipc_dirichlet_script: rotation about the unit ``axis``
+    through ``centre`` at ``omega`` rad/s, then translation at ``velocity``."""
+    a = np.asarray(axis, dtype=np.float64)
+    a = a / np.linalg.norm(a)
+    return np.concatenate([np.asarray(centre, dtype=np.float64), a, [float(omega)], np.asarray(velocity, dtype=np.float64)])
 
 
 def _static_dirichlet(mask):
@@ -121,6 +136,11 @@ def _static_dirichlet(mask):
         x_rest = x.copy()
         return lambda t: (mask, x_rest)
     return make
+
+
+def _static_script(mask):
+    """A fixed mask as one motionless group: targets equal the rest positions exactly."""
+    return np.where(mask, 0, -1).astype(np.int32), motion_row()[None, :]
 
 
 def two_cubes(n=8, seed=0, side=0.1, gap=2e-3, max_angle_deg=15.0, speed=1.0, E=1e5, nu=0.4, steps=50):
@@ -141,7 +161,8 @@ def two_cubes(n=8, seed=0, side=0.1, gap=2e-3, max_angle_deg=15.0, speed=1.0, E=
     v[len(lo):, 1] = -speed
     mask = np.zeros(nv, dtype=bool)
     mask[:len(lo)] = lo[:, 1] <= 1e-12
-    return _finish('two_cubes', [(lo, lt), (up, ut)], v, _static_dirichlet(mask), E=E, nu=nu, steps=steps,
+    return _finish('two_cubes', [(lo, lt), (up, ut)], v, _static_dirichlet(mask), script=_static_script(mask), E=E, nu=nu,
+                   steps=steps,
                    meta={'seed': seed, 'n': n, 'axis': axis.tolist(), 'angle': float(angle)})
 
 
@@ -169,7 +190,7 @@ def cube_lattice(m=6, n=6, seed=0, side=0.1, gap=2e-3, jitter=0.1, ground=(2.0, 
     nv = sum(len(p[0]) for p in parts)
     mask = np.zeros(nv, dtype=bool)
     mask[nv - len(gnd_x):] = True
-    return _finish('cube_lattice', parts, np.zeros((nv, 3)), _static_dirichlet(mask), steps=steps,
+    return _finish('cube_lattice', parts, np.zeros((nv, 3)), _static_dirichlet(mask), script=_static_script(mask), steps=steps,
                    meta={'seed': seed, 'm': m, 'n': n})
 
 
@@ -200,8 +221,12 @@ def twisted_bar(nx=400, ny=20, nz=20, size=(1.0, 0.05, 0.05), seed=0, jitter=1e-
             return ends, target
         return dirichlet
 
-    return _finish('twisted_bar', [(x, t)], np.zeros_like(x), make, E=E, nu=nu, dhat=dhat, gravity=0.0,
-                   steps=steps, meta={'seed': seed, 'nx': nx, 'ny': ny, 'nz': nz})
+    # the same schedule as rigid motions: the x<0 end turns about +x at -speed (its angle
+    # atan2(y, z) grows), the x>0 end at +speed
+    groups = np.where(ends, np.where(x[:, 0] < 0, 0, 1), -1).astype(np.int32)
+    motion = np.stack([motion_row(omega=-speed), motion_row(omega=speed)])
+    return _finish('twisted_bar', [(x, t)], np.zeros_like(x), make, script=(groups, motion), E=E, nu=nu, dhat=dhat,
+                   gravity=0.0, steps=steps, meta={'seed': seed, 'nx': nx, 'ny': ny, 'nz': nz})
 
 
 def predeform(scene, amplitude, seed=0):
@@ -242,7 +267,7 @@ def cube_stack(seed, side=0.1, gap=2e-3, min_cubes=1, max_cubes=8, min_hex=3, ma
     nv = sum(len(p[0]) for p in parts)
     mask = np.zeros(nv, dtype=bool)
     mask[nv - len(gnd_x):] = True
-    return _finish('cube_stack', parts, np.zeros((nv, 3)), _static_dirichlet(mask), steps=steps,
+    return _finish('cube_stack', parts, np.zeros((nv, 3)), _static_dirichlet(mask), script=_static_script(mask), steps=steps,
                    meta={'seed': seed, 'cubes': k})
 
 

@@ -7,8 +7,8 @@
  * constraint rows are [n][4] int32 (unused trailing ids zero); tets [T][4] int32.  `stream`
  * is a cudaStream_t (NULL for the legacy default stream).  Every function returns a status:
  * 0 ok, 1 capacity exceeded, 2 iteration limit, 3 non-finite value, 4 CUDA error,
- * 5 invalid argument.  The library allocates its own scratch inside a context and never
- * frees caller memory.  Calls on one context are not reentrant.
+ * 5 invalid argument, 6 file I/O error.  The library allocates its own scratch inside a
+ * context and never frees caller memory.  Calls on one context are not reentrant.
  */
 #ifndef FASTIPC_H
 #define FASTIPC_H
@@ -52,6 +52,15 @@ int fipc_compute_xn_and_xtilde(int n_verts, const double* x, const double* v, do
                                double* xtilde, void* stream);                 /* NEWTON_IPC.py:497-502 */
 int fipc_move_nodes(int n_verts, const unsigned char* fixed, const double* target, double* x, double* xtilde,
                     void* stream);                                             /* NEWTON_IPC.py:505-511 */
+/* Dirichlet schedule settings['dirichlet'](t) (projects/FastIPC/reader.py:154-357, consumed by
+ * move_nodes and solve_system, NEWTON_IPC.py:505-511, 758-763) evaluated on the device when it
+ * is a rigid motion of vertex groups.  group [V] int32 (< 0: free); motion [n_groups][10] =
+ * (centre c[3], unit axis a[3], omega rad/s, velocity u[3]); vertex i of group g gets
+ * target = c + R(a, omega t)(x_rest_i - c) + u t and fixed = 1.  Free vertices get fixed = 0 and
+ * target = x_rest.  Covers the reference's static masks (omega = 0, u = 0: target = x_rest
+ * exactly when c = 0), mat twist (reader.py:170-185) and translating faces (reader.py:336-345). */
+int fipc_dirichlet_script(int n_verts, const double* x_rest, const int* group, int n_groups, const double* motion, double t,
+                          unsigned char* fixed, double* target, void* stream);
 int fipc_apply_sol(int n_verts, const double* xprev, const double* sol, double alpha, double* x,
                    void* stream);                                              /* NEWTON_IPC.py:792-796 */
 int fipc_compute_v(int n_verts, const double* x, const double* xn, double dt, double* v,
@@ -188,6 +197,13 @@ int fipc_batch_solve_system(fipc_ctx* ctx, const unsigned char* fixed, const uns
                             int use_guess, double* sol, int* iters, int* n_failed, void* stream);
 /* the PCG shape the timing picked: rows per tile (= threads per block), grid, tiles, SpMV ms */
 int fipc_batch_pcg_shape(fipc_ctx* ctx, int* tile_rows, int* grid, int* n_tiles, float* spmv_ms);
+
+/* ---- per-frame output ---------------------------------------------------------------------- */
+/* write_image for 3D scenes (NEWTON_IPC.py:926-931): the OBJ file at path with one
+ * "v %.6f %.6f %.6f" line per vertex and one "f %d %d %d" line (1-based ids) per boundary
+ * triangle, byte for byte as the reference's Python formatting writes it.  HOST arrays
+ * x_h [V][3] and tris_h [F][3]; host code only (no GPU needed).  Status 6 on a file error. */
+int fipc_write_obj(const char* path, int n_verts, const double* x_h, int n_tris, const int* tris_h);
 
 /* ---- diagnostics -------------------------------------------------------------------------- */
 /* Time every launch of one kernel with CUDA events on its stream (1 PCG SpMV, 2 PCG update,
