@@ -274,3 +274,122 @@ def cube_stack(seed, side=0.1, gap=2e-3, min_cubes=1, max_cubes=8, min_hex=3, ma
 def cube_stacks(n_scenes=512, seed=0, **kw):
     """``n_scenes`` independent cube stacks with seeds seed, seed+1, ...: the batched workload."""
     return [cube_stack(seed + i, **kw) for i in range(n_scenes)]
+
+
+# ------------------------------------------------------------------------------ 2D scenes
+def tri_grid(nx, ny, size=(1.0, 1.0)):
+    """Vertices [V,2] f64 and counter-clockwise triangles [2*nx*ny, 3] i32 of the box
+    [0,size]: every quad split along its (i,j)-(i+1,j+1) diagonal."""
+    Nx, Ny = nx + 1, ny + 1
+    i, j = np.meshgrid(np.arange(Nx), np.arange(Ny), indexing='ij')
+    verts = np.stack([i.ravel() * (size[0] / nx), j.ravel() * (size[1] / ny)], axis=1).astype(np.float64)
+    qi, qj = np.meshgrid(np.arange(nx), np.arange(ny), indexing='ij')
+    a = (qi * Ny + qj).ravel()
+    b, c, d = a + Ny, a + Ny + 1, a + 1                    # (i+1,j), (i+1,j+1), (i,j+1)
+    tris = np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)], axis=1).reshape(-1, 3)
+    return verts, tris.astype(np.int32)
+
+
+def find_boundary_2d(tris):
+    """find_boundary of common/math/graph_tools.py:8-25 for triangles: a half-edge (i, j) without
+    its twin (j, i) gives the boundary edge [j, i], in triangle order."""
+    edges = set()
+    for i, j, k in tris.tolist():
+        edges.update([(i, j), (j, k), (k, i)])
+    pts, be = set(), []
+    for i, j, k in tris.tolist():
+        for a, b in ((i, j), (j, k), (k, i)):
+            if (b, a) not in edges:
+                pts.update([b, a])
+                be.append([b, a])
+    return np.array(sorted(pts), dtype=np.int32), np.array(be, dtype=np.int32).reshape(-1, 2)
+
+
+@dataclass
+class Scene2D:
+    name: str
+    x: np.ndarray                 # [V,2] f64 rest/initial positions
+    tris: np.ndarray              # [T,3] i32
+    v: np.ndarray                 # [V,2] f64 initial velocity
+    boundary_points: np.ndarray   # [Vs] i32
+    boundary_edges: np.ndarray    # [Es,2] i32
+    dirichlet: Callable           # t -> (mask[V] bool, target[V,2] f64)
+    E: float = 1e5
+    nu: float = 0.4
+    rho: float = 1000.0
+    dhat: float = 1e-3
+    dt: float = 0.01
+    gravity: float = -9.8
+    steps: int = 50
+    meta: dict = field(default_factory=dict)
+    x_init: np.ndarray = None
+
+    def initial_positions(self):
+        return self.x if self.x_init is None else self.x_init
+
+    @property
+    def n_verts(self):
+        return len(self.x)
+
+
+def _rot2(a):
+    return np.array([[np.cos(a), -np.sin(a)], [np.sin(a), np.cos(a)]])
+
+
+def two_squares_2d(n=4, seed=0, side=0.1, gap=2e-3, max_angle_deg=15.0, speed=1.0, E=1e5, nu=0.4, segment=True, steps=50):
+    """The 2D counterpart of ``two_cubes``: a lower square whose bottom row is fixed and an
+    upper square rotated by a seed-drawn angle (<= max_angle_deg), its lowest vertex ``gap``
+    above the lower one, moving at -speed m/s along y.  With ``segment``, a fixed ground
+    segment below the lower square is added as two boundary points and one boundary edge
+    without elements, as the reference's add_boundary does (projects/FastIPC/reader.py:87-101)."""
+    rng = np.random.default_rng(seed)
+    lo, lt = tri_grid(n, n, (side, side))
+    up, ut = tri_grid(n, n, (side, side))
+    ang = np.deg2rad(rng.uniform(-max_angle_deg, max_angle_deg))
+    c = np.full(2, side / 2)
+    up = (up - c) @ _rot2(ang).T + c
+    up[:, 1] += side + gap - up[:, 1].min()
+    x = np.concatenate([lo, up])
+    tris = np.concatenate([lt, ut + len(lo)]).astype(np.int32)
+    bp, be = find_boundary_2d(tris)
+    mask = np.zeros(len(x), dtype=bool)
+    mask[:len(lo)] = lo[:, 1] <= 1e-12
+    if segment:
+        k = len(x)
+        x = np.concatenate([x, [[-side, -gap], [2 * side, -gap]]])
+        bp = np.concatenate([bp, [k, k + 1]]).astype(np.int32)
+        be = np.concatenate([be, [[k, k + 1]]]).astype(np.int32)
+        mask = np.concatenate([mask, [True, True]])
+    v = np.zeros_like(x)
+    v[len(lo):len(lo) + len(up), 1] = -speed
+    x_rest = x.copy()
+    return Scene2D('two_squares_2d', x, tris, v, bp, be, lambda t: (mask, x_rest), E=E, nu=nu, steps=steps,
+                   meta={'seed': seed, 'n': n, 'angle': float(ang)})
+
+
+def square_stack_2d(k=8, n=16, seed=0, side=0.1, gap=2e-3, jitter=0.1, steps=50):
+    """A column of k squares (n x n quads, seed-drawn rotations up to 30 degrees and +-jitter
+    horizontal offsets) stacked with ``gap`` between bounding circles above a fixed ground
+    segment: the 2D workload for timing."""
+    rng = np.random.default_rng(seed)
+    base, bt = tri_grid(n, n, (side, side))
+    r = np.sqrt(2) * side / 2
+    xs, ts, y = [], [], gap + r
+    for _ in range(k):
+        R = _rot2(rng.uniform(-np.pi / 6, np.pi / 6))
+        ctr = np.array([rng.uniform(-jitter, jitter) * side, y])
+        ts.append(bt + sum(len(a) for a in xs))
+        xs.append((base - side / 2) @ R.T + ctr)
+        y += 2 * r + gap
+    x = np.concatenate(xs)
+    tris = np.concatenate(ts).astype(np.int32)
+    bp, be = find_boundary_2d(tris)
+    m = len(x)
+    x = np.concatenate([x, [[-1.0, 0.0], [1.0, 0.0]]])
+    bp = np.concatenate([bp, [m, m + 1]]).astype(np.int32)
+    be = np.concatenate([be, [[m, m + 1]]]).astype(np.int32)
+    mask = np.zeros(len(x), dtype=bool)
+    mask[m:] = True
+    x_rest = x.copy()
+    return Scene2D('square_stack_2d', x, tris, np.zeros_like(x), bp, be, lambda t: (mask, x_rest), steps=steps,
+                   meta={'seed': seed, 'k': k, 'n': n})

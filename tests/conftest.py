@@ -24,3 +24,9 @@ def unit_golden():
 def newton_golden():
     import numpy as np
     return np.load(os.path.join(GOLDEN, 'newton_two_cubes_n3.npz'))
+
+
+@pytest.fixture(scope='session')
+def newton2d_golden():
+    import numpy as np
+    return np.load(os.path.join(GOLDEN, 'newton2d_two_squares_n3.npz'))

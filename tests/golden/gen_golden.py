@@ -14,7 +14,7 @@ Sources of truth:
 Stand-ins (documented, not the reference's own code): Taichi's ``ti.svd`` (numpy SVD,
 rotation-variant), CHOLMOD's ``cholesky(A)(b)`` (scipy ``splu``, exact sparse LU).
 
-Usage:  python tests/golden/gen_golden.py [unit|newton|all]
+Usage:  python tests/golden/gen_golden.py [unit|newton|newton2d|all]
 """
 import ctypes
 import os
@@ -442,6 +442,141 @@ def gen_newton(n=3, steps=6, seed=0, record_iters=11, matrix_iters=(0, 2, 5)):
     print('wrote', f'newton_two_cubes_n{n}.npz')
 
 
+def gen_newton2d(n=3, steps=6, seed=0, record_iters=12):
+    """Run NEWTON_IPC.py's own functions with dim == 2 (fixed-corotated triangles, the
+    reference's default material) on a small two-square scene with a fixed ground segment and
+    record every step and every Newton iteration.
+
+    Source edits: dt = 0.01, E = 1e5, smaller MAX_LINEAR/MAX_C buffers, no GUI window.  d-hat^2
+    stays 1e-6.
+    The loop follows NEWTON_IPC.py:955-996 statement by statement.
+    """
+    from fastipc_gb300 import scenes
+    # pre-deformed start, as for the 3D fixture: at an exactly undeformed triangle the projected
+    # twist block of the reference's dP/dF depends on the sign of rounding noise
+    scene = scenes.predeform(scenes.two_squares_2d(n=n, seed=seed), 5e-4, seed)
+    subs = [
+        ('dt = 0.04', 'dt = 0.01'),
+        ('MAX_LINEAR = 50000000 if dim == 3 else 5000000', 'MAX_LINEAR = 100000'),
+        ('MAX_C = 100000', 'MAX_C = 5000'),
+        ('        E = 2.e4\n    nu = 0.4', '        E = 1.e5\n    nu = 0.4'),
+        # the 2D GUI window (images of write_image) is not part of the path: not created
+        ('    gui = ti.GUI("IPC", (768, 768), background_color=0x112F41)', '    gui = None'),
+    ]
+    _setup(subs)
+    import scipy.sparse.linalg as spla
+
+    reader = types.ModuleType('reader')
+    settings = {
+        'mesh_particles': scene.x.copy(), 'mesh_elements': scene.tris.copy(), 'dim': 2,
+        'gravity': scene.gravity, 'start_frame': 0,
+        'boundary': (set(scene.boundary_points.tolist()), scene.boundary_edges.copy(), np.array([[-1, -1, -1]])),
+        'dirichlet': scene.dirichlet, 'mesh_scale': 1.0, 'mesh_offset': [0., 0.],
+    }
+    reader.read = lambda: settings
+    reader.np = np
+    sys.modules['reader'] = reader
+    sys.modules['meshio'] = types.ModuleType('meshio')
+    chol = types.ModuleType('sksparse.cholmod')
+
+    def cholesky(A):
+        lu = spla.splu(A.tocsc())
+        return lambda b: lu.solve(b)
+    chol.cholesky = cholesky
+    sys.modules['sksparse'] = types.ModuleType('sksparse')
+    sys.modules['sksparse.cholmod'] = chol
+    os.chdir(tempfile.mkdtemp(prefix='fastipc_golden2d_'))
+    sys.argv = ['NEWTON_IPC.py', '2', '0']
+    import NEWTON_IPC as R
+
+    R.x.from_numpy(scene.x.astype(np.float64))
+    R.v.fill(0)
+    R.v.from_numpy(scene.v.astype(np.float64))
+    R.vertices.from_numpy(scene.tris.astype(np.int32))
+    R.boundary_points.from_numpy(scene.boundary_points.astype(np.int32))
+    R.boundary_edges.from_numpy(scene.boundary_edges.astype(np.int32))
+    R.compute_restT_and_m()
+    R.kappa = R.compute_adaptive_kappa() * 10
+    R.spatial_hash_inv_dx = 1.0 / R.compute_mean_of_boundary_edges()
+    R.save_x0()
+    R.x.from_numpy(scene.initial_positions().astype(np.float64))
+    rec = {'x_rest': scene.x, 'x_init': scene.initial_positions(), 'predeform': 5e-4, 'v_init': scene.v, 'tris': scene.tris, 'bpoints': scene.boundary_points,
+           'bedges': scene.boundary_edges, 'kappa': R.kappa, 'mean_edge': 1.0 / R.spatial_hash_inv_dx, 'mass': R.m.to_numpy(),
+           'dt': R.dt, 'dhat2': R.dHat2, 'n': n, 'seed': seed, 'steps': steps}
+    xs, vs, iters = [], [], []
+    it_global = 0
+    nd = 2 * len(scene.x)
+    for f in range(steps):
+        R.compute_xn_and_xTilde()
+        R.move_nodes(f * R.dt)
+        newton_iter = 0
+        while True:
+            newton_iter += 1
+            R.find_constraints()
+            R.data_row.fill(0)
+            R.data_col.fill(0)
+            R.data_val.fill(0)
+            R.data_rhs.fill(0)
+            R.data_sol.fill(0)
+            R.compute_hessian_and_gradient()
+            k = f'it{it_global}_'
+            if it_global < record_iters:
+                rec[k + 'x'] = R.x.to_numpy()
+                rec[k + 'xtilde'] = R.xTilde.to_numpy()
+                rec[k + 'PP'] = R.PP.to_numpy()[:R.n_PP[None]]
+                rec[k + 'PE'] = R.PE.to_numpy()[:R.n_PE[None]]
+                c = R.cnt[None]
+                import scipy.sparse
+                A = scipy.sparse.csr_matrix((R.data_val.to_numpy()[:c], (R.data_row.to_numpy()[:c], R.data_col.to_numpy()[:c])),
+                                            shape=(nd, nd))
+                A.sort_indices()
+                rec[k + 'A_data'], rec[k + 'A_indices'], rec[k + 'A_indptr'] = A.data, A.indices, A.indptr
+                rec[k + 'rhs'] = R.data_rhs.to_numpy()
+            R.solve_system(f * R.dt)
+            res = R.output_residual()
+            if it_global < record_iters:
+                rec[k + 'sol'] = R.data_sol.to_numpy()
+                rec[k + 'residual'] = res
+            if res < 1e-2 * R.dt:
+                it_global += 1
+                break
+            E0 = R.compute_energy()
+            R.save_xPrev()
+            alpha = R.compute_intersection_free_step_size()
+            alpha_ccd = alpha
+            R.apply_sol(alpha)
+            while R.check_collision():
+                alpha /= 2.0
+                R.apply_sol(alpha)
+            R.find_constraints()
+            E = R.compute_energy()
+            while E > E0:
+                alpha *= 0.5
+                R.apply_sol(alpha)
+                R.find_constraints()
+                E = R.compute_energy()
+            while R.check_collision():
+                alpha /= 2.0
+                R.apply_sol(alpha)
+            if it_global < record_iters:
+                rec[k + 'E0'] = E0
+                rec[k + 'alpha_ccd'] = alpha_ccd
+                rec[k + 'alpha'] = alpha
+                rec[k + 'E'] = E
+            it_global += 1
+            print(f'  step {f} newton {newton_iter} res {res:.3e} alpha {alpha:.4f}', flush=True)
+        R.compute_v()
+        xs.append(R.x.to_numpy())
+        vs.append(R.v.to_numpy())
+        iters.append(newton_iter)
+        print(f'step {f}: {newton_iter} newton iterations', flush=True)
+    rec['x_steps'] = np.array(xs)
+    rec['v_steps'] = np.array(vs)
+    rec['newton_iters'] = np.array(iters)
+    np.savez_compressed(os.path.join(HERE, f'newton2d_two_squares_n{n}.npz'), **rec)
+    print('wrote', f'newton2d_two_squares_n{n}.npz')
+
+
 if __name__ == '__main__':
     what = sys.argv[1] if len(sys.argv) > 1 else 'all'
     if what in ('unit', 'all'):
@@ -449,3 +584,5 @@ if __name__ == '__main__':
         gen_unit()
     if what in ('newton', 'all'):
         gen_newton()
+    if what in ('newton2d', 'all'):
+        gen_newton2d()

@@ -20,7 +20,7 @@ What it provides:
         through ctypes, with one ``double*`` per output (the reference ``a.so`` ABI);
     and module-level ``int``/``min``/``max``/``print`` that act elementwise on vectors
     (Taichi overloads these inside kernels).
-  * ``ti.svd`` as a rotation-variant SVD (det U = det V = +1, sign folded into sigma_3) built
+  * ``ti.svd`` as a rotation-variant SVD (det U = det V = +1, sign folded into the last sigma) built
     on numpy; Taichi's own svd is third-party and absent.
 
 Kernels run sequentially in Python; ``@ti.kernel`` parallel loops become plain loops.
@@ -105,7 +105,10 @@ class Mat(np.ndarray):
         return np.float64(np.dot(np.asarray(self).ravel(), np.asarray(o).ravel()))
 
     def cross(self, o):
-        return Mat(np.cross(np.asarray(self), np.asarray(o)))
+        a, b = np.asarray(self), np.asarray(o)
+        if a.shape == (2,):   # taichi's 2D cross product is the scalar a0 b1 - a1 b0
+            return np.float64(a[0] * b[1] - a[1] * b[0])
+        return Mat(np.cross(a, b))
 
     def outer_product(self, o):
         return Mat(np.outer(np.asarray(self), np.asarray(o)))
@@ -133,6 +136,9 @@ class Mat(np.ndarray):
         return Mat(np.asarray(self).T)
 
     def __getitem__(self, k):
+        # a taichi vector is an n x 1 matrix: v[i, 0] is v[i]
+        if self.ndim == 1 and isinstance(k, tuple) and len(k) == 2 and isinstance(k[1], (int, np.integer)) and k[1] == 0:
+            k = k[0]
         r = np.ndarray.__getitem__(self, k)
         if isinstance(r, np.ndarray) and r.ndim == 0:
             return r[()]
@@ -236,12 +242,13 @@ def cast(x, dtype):
 def svd(F):
     U, s, Vt = np.linalg.svd(np.asarray(F))
     V = Vt.T
+    k = len(s) - 1          # the sign goes into the last singular value (2x2 and 3x3)
     if np.linalg.det(U) < 0:
-        U[:, 2] *= -1
-        s[2] *= -1
+        U[:, k] *= -1
+        s[k] *= -1
     if np.linalg.det(V) < 0:
-        V[:, 2] *= -1
-        s[2] *= -1
+        V[:, k] *= -1
+        s[k] *= -1
     return Mat(U), Mat(np.diag(s)), Mat(V)
 
 

@@ -13,7 +13,7 @@ HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))
 def declared():
     src = open(HEADER).read()
     src = re.sub(r'/\*.*?\*/', '', src, flags=re.S)
-    return sorted(set(re.findall(r'\b(fipc_[a-z0-9_]+)\s*\(', src)))
+    return sorted(set(re.findall(r'\b(fipc(?:2d)?_[a-z0-9_]+)\s*\(', src)))
 
 
 def test_header_matches_binding():

