@@ -44,9 +44,10 @@ def parse():
     ap.add_argument('--profile-kernel', type=int, default=1, help='kernel timed for the roofline (1 = PCG SpMV)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--cpu-sample-pcg', type=int, default=100000)
-    ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes'],
+    ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes', 'stack2d'],
                     help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context; '
-                         'lattice: 216 cubes dropped on a ground box; cubes: two 8^3-hex cubes')
+                         'lattice: 216 cubes dropped on a ground box; cubes: two 8^3-hex cubes; '
+                         'stack2d: the 2D path, 16 squares of 16x16 quads on a ground segment')
     ap.add_argument('--scenes', type=int, default=512, help='scenes of the batch workload')
     ap.add_argument('--learned-steps', type=int, default=20,
                     help='steps run from the timed state with the inertial and the learned start (0: skip)')
@@ -215,6 +216,8 @@ def main():
     args = parse()
     if args.workload == 'batch':
         return main_batch(args)
+    if args.workload == 'stack2d':
+        return main_2d(args)
     if args.impl == 'reference':
         return run_reference(args)
     import numpy as np
@@ -431,6 +434,110 @@ def main_batch(args):
     if not args.no_cpu_baseline:
         v, sample, cores = batch_cpu(scs, args)
         out['cpu_baseline'] = {'value': v, 'unit': 'scene-steps/s', 'cores': cores, 'kind': 'port', 'sample': sample}
+    print(json.dumps(out), flush=True)
+    sim.close()
+
+
+STACK2D_METRIC = 'steps/s (2D: 16 squares, 8k triangles)'
+
+
+def main_2d(args):
+    """The 2D path (NEWTON_IPC.py with dim == 2): a column of 16 squares of 16 x 16 quads x2
+    triangles (4,626 vertices, 8,192 triangles, the size of the reference's 2D testcases) dropped
+    on a fixed ground segment; W warm-up
+    steps, K timed steps (CUDA events), e2e with the state through pinned host memory; the 2D
+    oracle times whole steps of the same scene from the same state on the host."""
+    from fastipc_gb300 import scenes as SC
+    rank = int(os.environ.get('RANK', '0'))
+    scene = SC.square_stack_2d(k=16, n=16, seed=0)
+    cfg = {'workload': '2D: 16 squares of 16x16 quads x2 fixed-corotated triangles on a ground segment (4626 verts, '
+                       '8192 tris), E=1e5 nu=0.4, dhat=1e-3, dt=0.01', 'tris': int(len(scene.tris)), 'verts': int(len(scene.x)),
+           'pcg_rtol': args.pcg_rtol, 'newton_tol': '|p|inf < 1e-2 dt', 'l2': 'working set below L2 (a 2D scene this size fits)'}
+
+    def cpu_steps(x0, v0, f0, budget_s=20.0):
+        from oracle import oracle2d as O2
+        o = O2.OracleSim2D(scene)
+        o.x, o.v = x0.copy(), v0.copy()
+        t0 = time.perf_counter()
+        n = 0
+        while n < args.steps and (n == 0 or time.perf_counter() - t0 < budget_s):
+            o.step(f0 + n)
+            n += 1
+        dt = time.perf_counter() - t0
+        return n / dt, f'{n} whole time steps ({f0}..{f0 + n - 1}) of the same scene from the same state (numpy + sparse LU)'
+
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        from oracle import oracle2d as O2
+        o = O2.OracleSim2D(scene)
+        for f in range(args.warmup):
+            o.step(f)
+        v, sample = cpu_steps(o.x, o.v, args.warmup)
+        print(json.dumps({'impl': 'reference', 'metric': STACK2D_METRIC, 'value': v, 'unit': 'steps/s', 'n_gpus': args.gpus,
+                          'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True, 'scaling': 'weak',
+                          'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
+                          'cpu_baseline': {'value': v, 'unit': 'steps/s', 'cores': 1, 'kind': 'port', 'sample': sample},
+                          'e2e': {'value': v, 'unit': 'steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}), flush=True)
+        return
+    import torch
+    from fastipc_gb300 import _native
+    from fastipc_gb300.build import build
+    from fastipc_gb300.newton2d import NewtonIPC2D
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    build()
+    sim = NewtonIPC2D(scene, device=dev, pcg_rtol=args.pcg_rtol)
+    f = 0
+    for _ in range(args.warmup):
+        sim.step(f)
+        f += 1
+    snap = (sim.x.clone(), sim.v.clone())
+    f0, n0 = f, len(sim.newton_iters)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _native.launch_count()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.step(f)
+            f += 1
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = _native.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    its = sim.newton_iters[n0:]
+    hx = torch.empty_like(snap[0], device='cpu').pin_memory()
+    hv = torch.empty_like(snap[1], device='cpu').pin_memory()
+    hx.copy_(snap[0])
+    hv.copy_(snap[1])
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    f = f0
+    for _ in range(args.steps):
+        sim.x.copy_(hx, non_blocking=True)
+        sim.v.copy_(hv, non_blocking=True)
+        sim.step(f)
+        hx.copy_(sim.x, non_blocking=True)
+        hv.copy_(sim.v, non_blocking=True)
+        f += 1
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1)
+    nbytes = 2 * sim.x.numel() * 8
+    out = {'metric': STACK2D_METRIC, 'value': args.steps / (ms / 1e3), 'unit': 'steps/s', 'n_gpus': 1, 'steps': args.steps,
+           'warmup': args.warmup, 'ms_per_step': ms / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
+           'newton_iters_per_step': sum(its) / len(its), 'ms_per_newton_iter': ms / max(sum(its), 1),
+           'pcg_iters_per_newton': sum(sim.pcg_iters[-sum(its):]) / max(sum(its), 1),
+           'e2e': {'value': args.steps / (e2e_ms / 1e3), 'unit': 'steps/s', 'h2d_bytes_per_step': nbytes, 'd2h_bytes_per_step': nbytes},
+           'gpu_launches': launches, 'clocks': clk.summary(), 'sections_s': {k: round(v, 4) for k, v in sim.timer.total.items()}}
+    if not args.no_cpu_baseline:
+        v, sample = cpu_steps(snap[0].cpu().numpy(), snap[1].cpu().numpy(), f0)
+        out['cpu_baseline'] = {'value': v, 'unit': 'steps/s', 'cores': 1, 'kind': 'port', 'sample': sample}
     print(json.dumps(out), flush=True)
     sim.close()
 

@@ -198,6 +198,57 @@ int fipc_batch_solve_system(fipc_ctx* ctx, const unsigned char* fixed, const uns
 /* the PCG shape the timing picked: rows per tile (= threads per block), grid, tiles, SpMV ms */
 int fipc_batch_pcg_shape(fipc_ctx* ctx, int* tile_rows, int* grid, int* n_tiles, float* spmv_ms);
 
+/* ---- the 2D path (NEWTON_IPC.py with dim == 2) ---------------------------------------------- */
+/* Positions [V][2] FP64, triangles [T][3] int32; fixed-corotated material (the reference's
+ * default import, common/physics/fixed_corotated.py); constraints between boundary points and
+ * boundary edges only: list 0 = PP rows (a, b), list 1 = PE rows (p, e0, e1), as [n][4] int32. */
+typedef struct fipc2d_ctx_impl fipc2d_ctx;
+
+/* compute_restT_and_m (NEWTON_IPC.py:485-494), adaptive kappa x10 (:116-124, :943), mean
+ * boundary edge (:127-134).  n_verts < 2^21.  Status 5 on an inverted or degenerate rest
+ * triangle. */
+int fipc2d_ctx_create(fipc2d_ctx** ctx, int n_verts, int n_tris, const int* tris_h, const double* x_rest_h,
+                      const double* lam_h, const double* mu_h, double rho, int n_bp, const int* bp_h, int n_be,
+                      const int* be_h, double dhat2, double dt);
+int fipc2d_ctx_destroy(fipc2d_ctx* ctx);
+int fipc2d_ctx_params(fipc2d_ctx* ctx, double* kappa_h, double* mean_edge_h);
+int fipc2d_ctx_set_kappa(fipc2d_ctx* ctx, double kappa);
+int fipc2d_ctx_mass(fipc2d_ctx* ctx, double* mass_h);
+int fipc2d_compute_xn_and_xtilde(int n_verts, const double* x, const double* v, double dt, double gravity, double* xn,
+                                 double* xtilde, void* stream);               /* NEWTON_IPC.py:497-502 */
+int fipc2d_move_nodes(int n_verts, const unsigned char* fixed, const double* target, double* x, double* xtilde,
+                      void* stream);                                           /* NEWTON_IPC.py:505-511 */
+int fipc2d_apply_sol(int n_verts, const double* xprev, const double* sol, double alpha, double* x,
+                     void* stream);                                            /* NEWTON_IPC.py:792-796 */
+int fipc2d_compute_v(int n_verts, const double* x, const double* xn, double dt, double* v,
+                     void* stream);                                            /* NEWTON_IPC.py:799-802 */
+/* Stateless kernels (tests): fixed-corotated triangles (NEWTON_IPC.py:577-624) -> energy E [T],
+ * gradient g [T][6], Hessian [T][6][6]; barrier rows of list type 0/1 (common/math/ipc.py:67-136,
+ * dim 2) -> E [n], g [n][2 nv], H [n][nv*nv][2][2]; point-edge CCD of explicit pairs
+ * xq/pq [n][3][2] (common/math/ipc.py:415-481). */
+int fipc2d_elements(int n_tris, const int* tris, const double* x, const double* ib, const double* vol, const double* lam,
+                    const double* mu, double dt, double* E, double* g, double* H, void* stream);
+int fipc2d_barrier_rows(int type, int n_rows, const int* rows, const double* x, double dhat2, double kappa, double* E,
+                        double* g, double* H, void* stream);
+int fipc2d_ccd_pairs(int n, const double* xq, const double* pq, double eta, double* toc, void* stream);
+/* find_constraints_2D_PE + dedup (NEWTON_IPC.py:159-179, 337-357): counts_h [2] */
+int fipc2d_find_constraints(fipc2d_ctx* ctx, const double* x, int* counts_h, void* stream);
+int fipc2d_get_constraints(fipc2d_ctx* ctx, int type, int* rows, void* stream);
+/* compute_hessian_and_gradient (NEWTON_IPC.py:736-747, dim 2): 2x2-block CSR and rhs -grad */
+int fipc2d_compute_hessian_and_gradient(fipc2d_ctx* ctx, const double* x, const double* xtilde, void* stream);
+int fipc2d_system_nnzb(fipc2d_ctx* ctx, int* nnzb_h);
+int fipc2d_export_system(fipc2d_ctx* ctx, int* row_ptr, int* col_idx, double* val, double* rhs, void* stream);
+/* solve_system (NEWTON_IPC.py:750-777) by block-Jacobi PCG to |r| <= rtol |b| */
+int fipc2d_solve_system(fipc2d_ctx* ctx, const unsigned char* fixed, double rtol, int maxit, double* sol, int* iters_h,
+                        void* stream);
+int fipc2d_output_residual(fipc2d_ctx* ctx, const double* sol, double* res_h, void* stream);    /* :805-812 */
+int fipc2d_compute_energy(fipc2d_ctx* ctx, const double* x, const double* xtilde, double* e_h, void* stream);  /* :514-542 */
+/* compute_filter_2D_PE (NEWTON_IPC.py:361-374, 456-468) */
+int fipc2d_compute_intersection_free_step_size(fipc2d_ctx* ctx, const double* x, const double* sol, double eta,
+                                               double* alpha_h, void* stream);
+/* check_collision_2D (NEWTON_IPC.py:843-854) */
+int fipc2d_check_collision(fipc2d_ctx* ctx, const double* x, int* hit_h, void* stream);
+
 /* ---- per-frame output ---------------------------------------------------------------------- */
 /* write_image for 3D scenes (NEWTON_IPC.py:926-931): the OBJ file at path with one
  * "v %.6f %.6f %.6f" line per vertex and one "f %d %d %d" line (1-based ids) per boundary
