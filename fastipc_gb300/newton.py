@@ -8,7 +8,9 @@ the reference's function names and semantics: ``compute_xn_and_xTilde``, ``move_
 NEWTON_IPC.py:955-999.  Every call goes to libfastipc.so; there is no other compute path.
 
 Differences from the reference, by design:
-  * the Newton direction comes from block-Jacobi PCG (``pcg_rtol``) instead of CHOLMOD;
+  * the Newton direction comes from PCG (``pcg_rtol``) instead of CHOLMOD; ``solver='direct'``
+    uses a sparse Cholesky factorisation as the reference does, and a PCG solve that reaches
+    ``pcg_maxit`` falls back to it (``direct_fallback``);
   * the Newton and line-search loops are bounded (``max_newton``, ``max_halvings``) and raise
     ``FastIPCError`` instead of spinning forever (NEWTON_IPC.py:961, 983, 988, 993 are
     unbounded).
@@ -48,7 +50,8 @@ class Timer:
 
 class NewtonIPC:
     def __init__(self, scene, device='cuda:0', pcg_rtol=1e-10, pcg_maxit=200000, eta=0.2, inversion_filter=True,
-                 max_newton=500, max_halvings=64, pcg_warm_start=False, coarse_agg=None, device_dirichlet=True):
+                 max_newton=500, max_halvings=64, pcg_warm_start=False, coarse_agg=None, device_dirichlet=True,
+                 solver='pcg', direct_fallback=True):
         self.scene = scene
         self.device = torch.device(device)
         torch.cuda.set_device(self.device)
@@ -57,6 +60,12 @@ class NewtonIPC:
         self.dhat2 = float(scene.dhat) ** 2
         self.eta = eta
         self.pcg_rtol, self.pcg_maxit = pcg_rtol, pcg_maxit
+        # 'pcg' (default) or 'direct' (sparse Cholesky, the reference's exact solve); with
+        # direct_fallback a PCG solve that reaches pcg_maxit is redone by the direct solver
+        if solver not in ('pcg', 'direct'):
+            raise FastIPCError(5, f'unknown solver {solver!r}')
+        self.solver, self.direct_fallback = solver, direct_fallback
+        self.direct_solves = 0
         self.inversion_filter = inversion_filter
         self.max_newton, self.max_halvings = max_newton, max_halvings
         self.timer = Timer()
@@ -230,13 +239,25 @@ class NewtonIPC:
             if guess:
                 self.data_sol.copy_(self._dir_hist[self._newton_k])
                 self.data_sol[self.fixed.bool()] = 0.0
-            st = N.lib().fipc_solve_system(self.ctx, dptr(self.fixed, torch.uint8), D(self.pcg_rtol), self.pcg_maxit, int(guess),
-                                           dptr(self.data_sol, F64), ctypes.byref(it), self._s())
-            check(st, 'solve_system')
-            self.pcg_iters.append(it.value)
+            if self.solver == 'direct':
+                self._solve_direct()
+                self.pcg_iters.append(0)
+            else:
+                st = N.lib().fipc_solve_system(self.ctx, dptr(self.fixed, torch.uint8), D(self.pcg_rtol), self.pcg_maxit,
+                                               int(guess), dptr(self.data_sol, F64), ctypes.byref(it), self._s())
+                if st == 2 and self.direct_fallback:      # PCG stopped at pcg_maxit
+                    self._solve_direct()
+                else:
+                    check(st, 'solve_system')
+                self.pcg_iters.append(it.value)
             if self.pcg_warm_start:
                 self._dir_hist[self._newton_k] = self.data_sol.clone()
             self._newton_k += 1
+
+    def _solve_direct(self):
+        check(N.lib().fipc_solve_system_direct(self.ctx, dptr(self.fixed, torch.uint8), dptr(self.data_sol, F64), None, self._s()),
+              'solve_system_direct')
+        self.direct_solves += 1
 
     def output_residual(self):
         r = D()

@@ -110,6 +110,12 @@ int fipc_solve_system(fipc_ctx* ctx, const unsigned char* fixed, double rtol, in
                       int* iters_h, void* stream);
 
 /* output_residual, NEWTON_IPC.py:805-812: max |sol| */
+/* solve_system by a sparse Cholesky factorisation instead of PCG: the reference's CHOLMOD solve
+ * (NEWTON_IPC.py:758-776) for the assembled system with its Dirichlet edit, for iterations
+ * where fipc_solve_system reaches its iteration limit.  The factorisation is cuSOLVER's, opened
+ * at run time: status 4 when it is not available, 3 when the system is not positive definite.
+ * nnz_h (may be NULL): scalar non-zeros factorised. */
+int fipc_solve_system_direct(fipc_ctx* ctx, const unsigned char* fixed, double* sol, int* nnz_h, void* stream);
 int fipc_output_residual(fipc_ctx* ctx, const double* sol, double* res_h, void* stream);
 
 /* compute_energy, NEWTON_IPC.py:514-542, over the lists of the last find_constraints */
