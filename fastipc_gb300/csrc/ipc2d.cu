@@ -14,6 +14,7 @@
 
 #include <string.h>
 
+#include <cooperative_groups.h>
 #include <cub/cub.cuh>
 #include <vector>
 
@@ -22,6 +23,8 @@
 #include "fc2d.cuh"
 
 namespace fipc {
+
+namespace cg = cooperative_groups;
 
 namespace {
 
@@ -464,6 +467,140 @@ __global__ void __launch_bounds__(T2) k2_pcg_dir(PCG2 a) {
     const size_t o = 2 * (size_t)i;
     a.p[o] = a.z[o] + be * a.p[o];
     a.p[o + 1] = a.z[o + 1] + be * a.p[o + 1];
+}
+
+// The whole PCG loop in one cooperative launch, for systems whose rows fit one CTA per SM:
+// small scenes are bound by per-kernel launch and tail latency, not by bandwidth.  Three grid
+// barriers per iteration; every CTA sums the per-CTA partials in the same fixed order, so all
+// CTAs hold the same scalars and take the same branch, and results are deterministic.  The
+// partials of p.q and of (r.z, |r|^2) live in separate arrays, so a fast CTA's next write never
+// meets a slow CTA's read.  part: 3 * gridDim.x doubles.
+__global__ void __launch_bounds__(T2) k2_pcg_coop(PCG2 a, const double* __restrict__ rhs, double rtol) {
+    cg::grid_group grid = cg::this_grid();
+    __shared__ double sh[T2];
+    const int G = gridDim.x;
+    const int stride = G * blockDim.x;
+    double* part_pq = a.part;
+    double* part_rz = a.part + G;
+    double* part_rr = a.part + 2 * G;
+    double rz = 0.0, bb = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nV; i += stride) {
+        const bool fx = a.fixed[i];
+        const double b0 = fx ? 0.0 : rhs[2 * (size_t)i], b1 = fx ? 0.0 : rhs[2 * (size_t)i + 1];
+        double m[4] = {1, 0, 0, 1};
+        if (!fx) {
+            const double* D = a.val + 4 * (size_t)a.dpos[i];
+            const double det = D[0] * D[3] - D[1] * D[2];
+            m[0] = D[3] / det;
+            m[1] = -D[1] / det;
+            m[2] = -D[2] / det;
+            m[3] = D[0] / det;
+        }
+        for (int k = 0; k < 4; ++k) a.minv[4 * (size_t)i + k] = m[k];
+        const double z0 = m[0] * b0 + m[1] * b1, z1 = m[2] * b0 + m[3] * b1;
+        const size_t o = 2 * (size_t)i;
+        a.x[o] = 0.0;
+        a.x[o + 1] = 0.0;
+        a.r[o] = b0;
+        a.r[o + 1] = b1;
+        a.z[o] = z0;
+        a.z[o + 1] = z1;
+        a.p[o] = z0;
+        a.p[o + 1] = z1;
+        rz += b0 * z0 + b1 * z1;
+        bb += b0 * b0 + b1 * b1;
+    }
+    {
+        const double s0 = bsum(rz, sh), s1 = bsum(bb, sh);
+        if (threadIdx.x == 0) {
+            part_rz[blockIdx.x] = s0;
+            part_rr[blockIdx.x] = s1;
+        }
+    }
+    grid.sync();
+    rz = sum_parts(part_rz, G, sh);
+    bb = sum_parts(part_rr, G, sh);
+    const double tol2 = rtol * rtol * bb;
+    if (bb == 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            a.flag[0] = 1;
+            a.flag[1] = 0;
+        }
+        return;
+    }
+    for (int it = 1; it <= a.maxit; ++it) {
+        // q = A p with the Dirichlet rows and columns replaced by the identity
+        double pq = 0.0;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nV; i += stride) {
+            const size_t o = 2 * (size_t)i;
+            const double p0 = a.p[o], p1 = a.p[o + 1];
+            double q0 = p0, q1 = p1;
+            if (!a.fixed[i]) {
+                q0 = q1 = 0.0;
+                for (int k = a.rp[i]; k < a.rp[i + 1]; ++k) {
+                    const int j = a.col[k];
+                    if (a.fixed[j]) continue;
+                    const double* B = a.val + 4 * (size_t)k;
+                    const double u0 = a.p[2 * (size_t)j], u1 = a.p[2 * (size_t)j + 1];
+                    q0 += B[0] * u0 + B[1] * u1;
+                    q1 += B[2] * u0 + B[3] * u1;
+                }
+            }
+            a.q[o] = q0;
+            a.q[o + 1] = q1;
+            pq += p0 * q0 + p1 * q1;
+        }
+        {
+            const double s0 = bsum(pq, sh);
+            if (threadIdx.x == 0) part_pq[blockIdx.x] = s0;
+        }
+        grid.sync();
+        const double alpha = rz / sum_parts(part_pq, G, sh);
+        double rz_new = 0.0, rr = 0.0;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nV; i += stride) {
+            const size_t o = 2 * (size_t)i;
+            a.x[o] += alpha * a.p[o];
+            a.x[o + 1] += alpha * a.p[o + 1];
+            const double r0 = a.r[o] - alpha * a.q[o], r1 = a.r[o + 1] - alpha * a.q[o + 1];
+            a.r[o] = r0;
+            a.r[o + 1] = r1;
+            const double* m = a.minv + 4 * (size_t)i;
+            const double z0 = m[0] * r0 + m[1] * r1, z1 = m[2] * r0 + m[3] * r1;
+            a.z[o] = z0;
+            a.z[o + 1] = z1;
+            rz_new += r0 * z0 + r1 * z1;
+            rr += r0 * r0 + r1 * r1;
+        }
+        {
+            const double s0 = bsum(rz_new, sh), s1 = bsum(rr, sh);
+            if (threadIdx.x == 0) {
+                part_rz[blockIdx.x] = s0;
+                part_rr[blockIdx.x] = s1;
+            }
+        }
+        grid.sync();
+        rz_new = sum_parts(part_rz, G, sh);
+        rr = sum_parts(part_rr, G, sh);
+        if (rr <= tol2) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) {
+                a.flag[0] = 1;
+                a.flag[1] = it;
+            }
+            return;
+        }
+        const double beta = rz_new / rz;
+        rz = rz_new;
+        for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nV; i += stride) {
+            const size_t o = 2 * (size_t)i;
+            a.p[o] = a.z[o] + beta * a.p[o];
+            a.p[o + 1] = a.z[o + 1] + beta * a.p[o + 1];
+        }
+        grid.sync();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.flag[0] = 2;
+        a.flag[1] = a.maxit;
+    }
 }
 
 // ---------------------------------------------------------------- energy, residual, CCD, collision
@@ -1093,7 +1230,7 @@ int fipc2d_solve_system(fipc2d_ctx_impl* h, const unsigned char* fixed, double r
     cudaStream_t s = (cudaStream_t)stream;
     const int nb = nb2(c->nV, T2);
     const size_t n2 = 2ull * c->nV;
-    if (c->pvec.ensure(8 * (4 * n2 + 4ull * c->nV)) || c->ppart.ensure(16ull * nb + 64) || c->pflag.ensure(64 + 16)) return FIPC_ERR_CUDA;
+    if (c->pvec.ensure(8 * (4 * n2 + 4ull * c->nV)) || c->ppart.ensure(24ull * nb + 64) || c->pflag.ensure(64 + 16)) return FIPC_ERR_CUDA;
     PCG2 a;
     a.nV = c->nV;
     a.rp = c->row_ptr.as<int>();
@@ -1113,9 +1250,27 @@ int fipc2d_solve_system(fipc2d_ctx_impl* h, const unsigned char* fixed, double r
     a.flag = (int*)(c->pflag.as<char>() + 64);
     a.maxit = maxit;
     FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 16, s));
+    int hf[2] = {0, 0};
+    // one cooperative launch when the rows fit one CTA per SM
+    int dev = 0, nsm = 0, per = 0;
+    FIPC_CUDA(cudaGetDevice(&dev));
+    FIPC_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    FIPC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k2_pcg_coop, T2, 0));
+    if (maxit > 0 && per >= 1 && nb <= nsm) {
+        const double* rhs = c->rhs.as<double>();
+        void* args[] = {&a, &rhs, &rtol};
+        if (cudaLaunchCooperativeKernel((const void*)k2_pcg_coop, dim3(nb), dim3(T2), args, 0, s) == cudaSuccess) {
+            FIPC_LAUNCHED();
+            FIPC_CUDA(cudaMemcpyAsync(hf, a.flag, 8, cudaMemcpyDeviceToHost, s));
+            FIPC_CUDA(cudaStreamSynchronize(s));
+            FIPC_CUDA(cudaGetLastError());
+            if (iters_h) *iters_h = hf[1];
+            return hf[0] == 1 ? FIPC_OK : FIPC_ERR_ITERATION;
+        }
+        cudaGetLastError();   // not launchable here: the multi-kernel path below
+    }
     k2_pcg_start<<<nb, T2, 0, s>>>(a, c->rhs.as<double>(), rtol);
     FIPC_LAUNCHED();
-    int hf[2] = {0, 0};
     // whole chunks: the iteration that converges or reaches maxit turns the rest of its chunk
     // into early exits
     const bool graph = maxit > 0 && pcg_graph(c, a, nb);
