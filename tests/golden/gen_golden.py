@@ -503,6 +503,13 @@ def gen_newton2d(n=3, steps=6, seed=0, record_iters=12):
     rec = {'x_rest': scene.x, 'x_init': scene.initial_positions(), 'predeform': 5e-4, 'v_init': scene.v, 'tris': scene.tris, 'bpoints': scene.boundary_points,
            'bedges': scene.boundary_edges, 'kappa': R.kappa, 'mean_edge': 1.0 / R.spatial_hash_inv_dx, 'mass': R.m.to_numpy(),
            'dt': R.dt, 'dhat2': R.dHat2, 'n': n, 'seed': seed, 'steps': steps}
+    # the reference's own boundary extraction (graph_tools.py:8-25) on the scenes' triangles
+    from common.math.graph_tools import find_boundary as ref_find_boundary
+    rbp, rbe, _ = ref_find_boundary(scene.tris)
+    rec['ref_bpoints'], rec['ref_bedges'] = np.array(sorted(rbp)), np.asarray(rbe)
+    stack = scenes.square_stack_2d(k=3, n=4, seed=1)
+    rbp, rbe, _ = ref_find_boundary(stack.tris)
+    rec['stack_tris'], rec['stack_ref_bpoints'], rec['stack_ref_bedges'] = stack.tris, np.array(sorted(rbp)), np.asarray(rbe)
     xs, vs, iters = [], [], []
     it_global = 0
     nd = 2 * len(scene.x)

@@ -40,6 +40,21 @@ def test_scene_matches_fixture(newton2d_golden):
     np.testing.assert_array_equal(sc.initial_positions(), g['x_init'])
 
 
+def test_boundary_matches_reference(newton2d_golden):
+    """scenes.find_boundary_2d against the reference's graph_tools.find_boundary (run on the
+    same triangles when the fixture was made): the same points and the same oriented edges in
+    the same order."""
+    g = newton2d_golden
+    for tris, pts, edges in ((g['tris'], g['ref_bpoints'], g['ref_bedges']),
+                             (g['stack_tris'], g['stack_ref_bpoints'], g['stack_ref_bedges'])):
+        bp, be = scenes.find_boundary_2d(tris)
+        np.testing.assert_array_equal(bp, pts)
+        np.testing.assert_array_equal(be, edges.reshape(-1, 2))
+    sc = golden_scene2d(g)
+    n = len(g['ref_bedges'])
+    np.testing.assert_array_equal(sc.boundary_edges[:n], g['ref_bedges'].reshape(-1, 2))
+
+
 def test_setup(newton2d_golden, run):
     sim, _ = run
     g = newton2d_golden
