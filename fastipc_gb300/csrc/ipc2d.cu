@@ -34,6 +34,10 @@ constexpr int P2_RED = 304;   // fixed reduction grid (2 x 152 SMs)
 
 inline int nb2(long long n, int b) { return (int)((n + b - 1) / b); }
 
+// positions are read as one 16-byte double2 per vertex and rows as int4: their base addresses
+// must be 16-byte aligned (every fresh device allocation is; a view at an odd offset is not)
+inline bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
 __device__ __forceinline__ double2 ld2(const double* x, int i) { return *reinterpret_cast<const double2*>(x + 2 * (size_t)i); }
 
 // fixed-tree block sum (blockDim.x == T2)
@@ -1040,7 +1044,7 @@ int fipc2d_compute_v(int n_verts, const double* x, const double* xn, double dt, 
 
 int fipc2d_elements(int n_tris, const int* tris, const double* x, const double* ib, const double* vol, const double* lam,
                     const double* mu, double dt, double* E, double* g, double* H, void* stream) {
-    if (n_tris < 0 || !tris || !x || !ib || !vol || !lam || !mu) return FIPC_ERR_ARGUMENT;
+    if (n_tris < 0 || !tris || !x || !ib || !vol || !lam || !mu || !al16(x)) return FIPC_ERR_ARGUMENT;
     if (!n_tris) return FIPC_OK;
     k2_elements<<<nb2(n_tris, T2), T2, 0, (cudaStream_t)stream>>>(n_tris, tris, x, ib, vol, lam, mu, dt * dt, E, g, H);
     FIPC_LAUNCHED();
@@ -1050,7 +1054,8 @@ int fipc2d_elements(int n_tris, const int* tris, const double* x, const double* 
 
 int fipc2d_barrier_rows(int type, int n_rows, const int* rows, const double* x, double dhat2, double kappa, double* E, double* g,
                         double* H, void* stream) {
-    if ((type != 0 && type != 1) || n_rows < 0 || !rows || !x || ((g == nullptr) != (H == nullptr))) return FIPC_ERR_ARGUMENT;
+    if ((type != 0 && type != 1) || n_rows < 0 || !rows || !x || ((g == nullptr) != (H == nullptr)) || !al16(x) || !al16(rows))
+        return FIPC_ERR_ARGUMENT;
     if (!n_rows) return FIPC_OK;
     k2_barrier<<<nb2(n_rows, 128), 128, 0, (cudaStream_t)stream>>>(type, n_rows, (const int4*)rows, x, dhat2, kappa, E, g, H);
     FIPC_LAUNCHED();
@@ -1068,7 +1073,7 @@ int fipc2d_ccd_pairs(int n, const double* xq, const double* pq, double eta, doub
 }
 
 int fipc2d_find_constraints(fipc2d_ctx_impl* h, const double* x, int* counts_h, void* stream) {
-    if (!h || !x) return FIPC_ERR_ARGUMENT;
+    if (!h || !x || !al16(x)) return FIPC_ERR_ARGUMENT;
     Ctx2* c = &h->c;
     cudaStream_t s = (cudaStream_t)stream;
     if (c->cnt_d.ensure(16) || c->scal.ensure(64)) return FIPC_ERR_CUDA;
@@ -1137,7 +1142,7 @@ int fipc2d_get_constraints(fipc2d_ctx_impl* h, int type, int* rows, void* stream
 }
 
 int fipc2d_compute_hessian_and_gradient(fipc2d_ctx_impl* h, const double* x, const double* xtilde, void* stream) {
-    if (!h || !x || !xtilde) return FIPC_ERR_ARGUMENT;
+    if (!h || !x || !xtilde || !al16(x)) return FIPC_ERR_ARGUMENT;
     Ctx2* c = &h->c;
     cudaStream_t s = (cudaStream_t)stream;
     const int nPP = c->h_counts[0], nPE = c->h_counts[1];
@@ -1307,7 +1312,7 @@ int fipc2d_output_residual(fipc2d_ctx_impl* h, const double* sol, double* res_h,
 }
 
 int fipc2d_compute_energy(fipc2d_ctx_impl* h, const double* x, const double* xtilde, double* e_h, void* stream) {
-    if (!h || !x || !xtilde || !e_h) return FIPC_ERR_ARGUMENT;
+    if (!h || !x || !xtilde || !e_h || !al16(x)) return FIPC_ERR_ARGUMENT;
     Ctx2* c = &h->c;
     cudaStream_t s = (cudaStream_t)stream;
     if (c->epart.ensure(8ull * P2_RED) || c->eout.ensure(16)) return FIPC_ERR_CUDA;
@@ -1325,7 +1330,7 @@ int fipc2d_compute_energy(fipc2d_ctx_impl* h, const double* x, const double* xti
 
 int fipc2d_compute_intersection_free_step_size(fipc2d_ctx_impl* h, const double* x, const double* sol, double eta, double* alpha_h,
                                                void* stream) {
-    if (!h || !x || !sol || !alpha_h) return FIPC_ERR_ARGUMENT;
+    if (!h || !x || !sol || !alpha_h || !al16(x) || !al16(sol)) return FIPC_ERR_ARGUMENT;
     Ctx2* c = &h->c;
     cudaStream_t s = (cudaStream_t)stream;
     if (c->eout.ensure(16)) return FIPC_ERR_CUDA;
@@ -1343,7 +1348,7 @@ int fipc2d_compute_intersection_free_step_size(fipc2d_ctx_impl* h, const double*
 }
 
 int fipc2d_check_collision(fipc2d_ctx_impl* h, const double* x, int* hit_h, void* stream) {
-    if (!h || !x || !hit_h) return FIPC_ERR_ARGUMENT;
+    if (!h || !x || !hit_h || !al16(x)) return FIPC_ERR_ARGUMENT;
     Ctx2* c = &h->c;
     cudaStream_t s = (cudaStream_t)stream;
     if (c->cnt_d.ensure(16)) return FIPC_ERR_CUDA;

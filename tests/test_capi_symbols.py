@@ -31,3 +31,20 @@ def test_status_strings():
     lib.fipc_status_string.restype = ctypes.c_char_p
     assert lib.fipc_status_string(0) == b'ok'
     assert lib.fipc_status_string(5) == b'invalid argument'
+
+
+def test_2d_entry_points_reject_misaligned_positions():
+    """The 2D kernels read a vertex as one 16-byte load: a position array that does not start on
+    a 16-byte boundary is rejected with status 5 before anything reaches the device (host logic
+    only, no compute call)."""
+    import numpy as np
+    lib = ctypes.CDLL(build())
+    buf = np.zeros(64, dtype=np.float64)
+    base = buf.ctypes.data
+    odd = ctypes.c_void_p(base + (8 if base % 16 == 0 else 0))     # 8 mod 16
+    tris = np.zeros(3, dtype=np.int32)
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    assert lib.fipc2d_elements(1, P(tris), odd, P(buf), P(buf), P(buf), P(buf), ctypes.c_double(0.01), None, None, None,
+                               None) == 5
+    assert lib.fipc2d_barrier_rows(0, 1, P(tris), odd, ctypes.c_double(1e-6), ctypes.c_double(1.0), None, None, None,
+                                   None) == 5
