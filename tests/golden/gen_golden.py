@@ -526,24 +526,24 @@ def gen_newton2d(n=3, steps=6, seed=0, record_iters=12):
             R.data_rhs.fill(0)
             R.data_sol.fill(0)
             R.compute_hessian_and_gradient()
-            k = f'it{it_global}_'
-            if it_global < record_iters:
-                rec[k + 'x'] = R.x.to_numpy()
-                rec[k + 'xtilde'] = R.xTilde.to_numpy()
-                rec[k + 'PP'] = R.PP.to_numpy()[:R.n_PP[None]]
-                rec[k + 'PE'] = R.PE.to_numpy()[:R.n_PE[None]]
-                c = R.cnt[None]
-                import scipy.sparse
-                A = scipy.sparse.csr_matrix((R.data_val.to_numpy()[:c], (R.data_row.to_numpy()[:c], R.data_col.to_numpy()[:c])),
-                                            shape=(nd, nd))
-                A.sort_indices()
-                rec[k + 'A_data'], rec[k + 'A_indices'], rec[k + 'A_indptr'] = A.data, A.indices, A.indptr
-                rec[k + 'rhs'] = R.data_rhs.to_numpy()
+            # the first record_iters iterations under it{i}_ (every consumer), the rest under xt{i}_
+            # with '_res' for the residual (oracle tests only)
+            k = f'it{it_global}_' if it_global < record_iters else f'xt{it_global}_'
+            rec[k + 'x'] = R.x.to_numpy()
+            rec[k + 'xtilde'] = R.xTilde.to_numpy()
+            rec[k + 'PP'] = R.PP.to_numpy()[:R.n_PP[None]]
+            rec[k + 'PE'] = R.PE.to_numpy()[:R.n_PE[None]]
+            c = R.cnt[None]
+            import scipy.sparse
+            A = scipy.sparse.csr_matrix((R.data_val.to_numpy()[:c], (R.data_row.to_numpy()[:c], R.data_col.to_numpy()[:c])),
+                                        shape=(nd, nd))
+            A.sort_indices()
+            rec[k + 'A_data'], rec[k + 'A_indices'], rec[k + 'A_indptr'] = A.data, A.indices, A.indptr
+            rec[k + 'rhs'] = R.data_rhs.to_numpy()
             R.solve_system(f * R.dt)
             res = R.output_residual()
-            if it_global < record_iters:
-                rec[k + 'sol'] = R.data_sol.to_numpy()
-                rec[k + 'residual'] = res
+            rec[k + 'sol'] = R.data_sol.to_numpy()
+            rec[k + ('residual' if it_global < record_iters else 'res')] = res
             if res < 1e-2 * R.dt:
                 it_global += 1
                 break
@@ -565,11 +565,10 @@ def gen_newton2d(n=3, steps=6, seed=0, record_iters=12):
             while R.check_collision():
                 alpha /= 2.0
                 R.apply_sol(alpha)
-            if it_global < record_iters:
-                rec[k + 'E0'] = E0
-                rec[k + 'alpha_ccd'] = alpha_ccd
-                rec[k + 'alpha'] = alpha
-                rec[k + 'E'] = E
+            rec[k + 'E0'] = E0
+            rec[k + 'alpha_ccd'] = alpha_ccd
+            rec[k + 'alpha'] = alpha
+            rec[k + 'E'] = E
             it_global += 1
             print(f'  step {f} newton {newton_iter} res {res:.3e} alpha {alpha:.4f}', flush=True)
         R.compute_v()

@@ -1,7 +1,7 @@
 """The 2D oracle against the reference's own 2D driver (NEWTON_IPC.py with dim == 2, run
 through the Taichi stand-in; fixture tests/golden/newton2d_two_squares_n3.npz) on two squares
-with a fixed ground segment (no GPU), and its element and CCD pieces against the reference's
-native a.so where that library is available.
+with a fixed ground segment (no GPU): all 32 Newton iterations of six steps, point-edge and
+point-point contact, CCD-limited line searches.
 
 Bars: constraint lists exact; gradient and assembled Hessian 1e-9 relative to their largest
 entry; energy 1e-10 relative; CCD step 1e-6; Newton iteration counts equal; positions after
@@ -83,6 +83,36 @@ def test_iterations(newton2d_golden, run):
             assert abs(r['alpha_ccd'] - float(g[k + 'alpha_ccd'])) <= 1e-6, i
             assert abs(r['alpha'] - float(g[k + 'alpha'])) <= 1e-6, i
     assert n_pe > 0   # contact is exercised
+
+
+def test_later_iterations_with_point_point_rows(newton2d_golden, run):
+    """The iterations after the first twelve (fixture keys xt{i}_), which include the
+    point-point rows of steps 3-4, evaluated at the reference's own iterates: lists, system,
+    direction, energy and CCD step."""
+    g = newton2d_golden
+    sim, _ = run
+    n = 2 * len(sim.x)
+    extra = sorted(int(k[2:].split('_')[0]) for k in g.files if k.startswith('xt') and k.endswith('_res'))
+    assert len(extra) >= 10
+    n_pp = 0
+    for i in extra:
+        k = f'xt{i}_'
+        sim.x, sim.xTilde = g[k + 'x'].copy(), g[k + 'xtilde']
+        sim.find_constraints()
+        np.testing.assert_array_equal(sim.PP, g[k + 'PP'].reshape(-1, 2), err_msg=f'iteration {i} PP')
+        np.testing.assert_array_equal(sim.PE, g[k + 'PE'].reshape(-1, 3), err_msg=f'iteration {i} PE')
+        n_pp += len(sim.PP)
+        sim.compute_hessian_and_gradient()
+        A_ref = sp.csr_matrix((g[k + 'A_data'], g[k + 'A_indices'], g[k + 'A_indptr']), shape=(n, n))
+        assert abs(sim.A - A_ref).max() <= 1e-9 * abs(A_ref).max(), i
+        assert np.abs(sim.rhs - g[k + 'rhs']).max() <= 1e-9 * np.abs(g[k + 'rhs']).max(), i
+        sol = sim.solve_system(0.0)
+        assert np.abs(sol - g[k + 'sol']).max() <= 1e-8 * np.abs(g[k + 'sol']).max(), i
+        if k + 'E0' in g.files:
+            assert abs(sim.compute_energy() - float(g[k + 'E0'])) <= 1e-10 * abs(float(g[k + 'E0'])), i
+            sim.sol = g[k + 'sol']
+            assert abs(sim.compute_intersection_free_step_size() - float(g[k + 'alpha_ccd'])) <= 1e-6, i
+    assert n_pp > 0
 
 
 def test_matrices(newton2d_golden, run):
