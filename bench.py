@@ -182,6 +182,23 @@ def cpu_baseline(scene, newton_per_step, pcg_per_newton, args):
             'ms_per_newton_iter': 1e3 * t_newton}
 
 
+def max_over_ranks(ms, dist, device):
+    """The slowest rank's time (ms) of a timed region: an all-reduce MAX over the ranks (the
+    value itself for one process)."""
+    if dist is None:
+        return float(ms)
+    import torch
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world, steps, ms_max):
+    """Whole-job steps/s of `world` independent replicas that each ran `steps` steps, timed by
+    the slowest one."""
+    return world * steps / (ms_max / 1e3)
+
+
 def run_reference(args):
     """CPU oracle, whole time steps of the same scene (rank 0 only)."""
     rank = int(os.environ.get('RANK', '0'))
@@ -271,12 +288,8 @@ def main():
     L.fipc_profile_enable(0)
     newton = sim.newton_iters[n_newton0:]
     pcg = sim.pcg_iters[n_pcg0:]
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * args.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks(ms, dist, dev)
+    value = replica_throughput(world, args.steps, ms_max)
 
     # e2e: the same steps again from the same state, state round-tripped through pinned host memory
     hx = torch.empty_like(snap[0], device='cpu').pin_memory()
@@ -298,11 +311,7 @@ def main():
         f += 1
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    if dist is not None:
-        t = torch.tensor([e2e_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     nbytes = 2 * sim.x.numel() * 8
 
     learned = learned_leg(sim, snap, f0, args) if args.learned_steps > 0 and args.workload == 'bar' else None
