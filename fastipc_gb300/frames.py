@@ -57,21 +57,27 @@ class FrameWriter:
     ``submit(f, x, v)`` returns as soon as the frame is queued; ``flush()`` waits for every
     queued frame and re-raises the first error a write met.  ``depth`` frames can be in
     flight; a further submit waits for the oldest one.  x and v may be CUDA or CPU tensors (or
-    numpy arrays).
+    numpy arrays) of shape [V, dim].  With dim 2 only caches are written: the reference's 2D
+    write_image draws into a window instead of writing a file.
     """
 
-    def __init__(self, directory, triangles, n_verts, obj=True, cache=True, depth=2):
+    def __init__(self, directory, triangles, n_verts, obj=True, cache=True, depth=2, dim=3):
+        if dim not in (2, 3):
+            raise ValueError('dim must be 2 or 3')
+        if dim == 2 and obj:
+            raise ValueError('OBJ frames are written for 3D scenes only')
         self.directory = directory
         self.obj, self.cache = obj, cache
-        self.tris = np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
+        self.dim = dim
+        self.tris = None if triangles is None else np.ascontiguousarray(triangles, dtype=np.int32).reshape(-1, 3)
         self.n = int(n_verts)
         for sub, on in (('objs', obj), ('caches', cache)):
             if on:
                 os.makedirs(os.path.join(directory, sub), exist_ok=True)
         self.cuda = torch.cuda.is_available()
         pin = self.cuda
-        self._host = [(torch.empty((self.n, 3), dtype=torch.float64, pin_memory=pin),
-                       torch.empty((self.n, 3), dtype=torch.float64, pin_memory=pin)) for _ in range(depth)]
+        self._host = [(torch.empty((self.n, dim), dtype=torch.float64, pin_memory=pin),
+                       torch.empty((self.n, dim), dtype=torch.float64, pin_memory=pin)) for _ in range(depth)]
         self._dev = [None] * depth          # device snapshots, made on first CUDA submit
         self._free = queue.Queue()
         for k in range(depth):
@@ -92,14 +98,14 @@ class FrameWriter:
         done = None
         if isinstance(x, torch.Tensor) and x.is_cuda:
             if self._dev[k] is None:
-                self._dev[k] = (torch.empty((self.n, 3), dtype=torch.float64, device=x.device),
-                                torch.empty((self.n, 3), dtype=torch.float64, device=x.device))
+                self._dev[k] = (torch.empty((self.n, self.dim), dtype=torch.float64, device=x.device),
+                                torch.empty((self.n, self.dim), dtype=torch.float64, device=x.device))
             if self._copy_stream is None:
                 self._copy_stream = torch.cuda.Stream(device=x.device)
             dx, dv = self._dev[k]
             main = torch.cuda.current_stream(x.device)
-            dx.copy_(x.reshape(-1, 3))          # snapshot on the simulation stream
-            dv.copy_(v.reshape(-1, 3))
+            dx.copy_(x.reshape(-1, self.dim))   # snapshot on the simulation stream
+            dv.copy_(v.reshape(-1, self.dim))
             snap = torch.cuda.Event()
             snap.record(main)
             with torch.cuda.stream(self._copy_stream):
@@ -109,8 +115,8 @@ class FrameWriter:
                 done = torch.cuda.Event()
                 done.record(self._copy_stream)
         else:
-            hx.copy_(torch.as_tensor(np.asarray(x, dtype=np.float64)).reshape(-1, 3))
-            hv.copy_(torch.as_tensor(np.asarray(v, dtype=np.float64)).reshape(-1, 3))
+            hx.copy_(torch.as_tensor(np.asarray(x, dtype=np.float64)).reshape(-1, self.dim))
+            hv.copy_(torch.as_tensor(np.asarray(v, dtype=np.float64)).reshape(-1, self.dim))
         self._jobs.put((f, k, done, self.obj if obj is None else obj, self.cache if cache is None else cache))
 
     def _run(self):

@@ -186,6 +186,36 @@ class NewtonIPC2D:
         check(N.lib().fipc2d_compute_v(self.nV, dptr(self.x, F64), dptr(self.xn, F64), D(self.dt), dptr(self.v, F64), self._s()),
               'compute_v')
 
+    def set_state(self, x, v):
+        """Positions and velocities [V,2] (host or device), as the restart of NEWTON_IPC.py:949-953
+        loads them."""
+        self.x.copy_(torch.as_tensor(np.asarray(x, dtype=np.float64) if not isinstance(x, torch.Tensor) else x).reshape(-1, 2))
+        self.v.copy_(torch.as_tensor(np.asarray(v, dtype=np.float64) if not isinstance(v, torch.Tensor) else v).reshape(-1, 2))
+
+    def run(self, n_frames, directory=None, start_frame=0):
+        """The reference's main loop for dim 2 (NEWTON_IPC.py:947-1003) for n_frames time steps.
+        With a directory, the state after every step goes to caches/%06d.p as the reference
+        writes it (pickled [x, v]); start_frame > 0 restarts from caches/{start_frame:06d}.p.
+        The 2D write_image draws into a window and is not reproduced.  Returns the Newton
+        iteration count of every step."""
+        from . import frames
+        writer = frames.FrameWriter(directory, None, self.nV, obj=False, cache=True, dim=2) if directory is not None else None
+        try:
+            if start_frame > 0:
+                x, v = frames.load_cache(frames.cache_path(directory, start_frame))
+                self.set_state(x, v)
+            its = []
+            for f in range(start_frame, start_frame + n_frames):
+                its.append(self.step(f))
+                if writer is not None:
+                    writer.submit(f + 1, self.x, self.v)
+            if writer is not None:
+                writer.flush()
+        finally:
+            if writer is not None:
+                writer.close()
+        return its
+
     # ------------------------------------------------------------------ the time step
     def step(self, f, record=None):
         """One time step (NEWTON_IPC.py:955-999); returns the Newton iteration count."""

@@ -155,3 +155,21 @@ def test_static_script_is_exact(make):
         ref_mask, ref_tgt = sc.dirichlet(t)
         assert np.array_equal(mask, ref_mask)
         assert np.array_equal(tgt, ref_tgt)
+
+
+def test_frame_writer_2d_caches(tmp_path):
+    """dim 2: caches only, [V,2] arrays as the reference's 2D driver pickles them."""
+    rng = np.random.default_rng(8)
+    d = str(tmp_path / 'run2d')
+    w = frames.FrameWriter(d, None, 11, obj=False, dim=2)
+    states = [(rng.normal(size=(11, 2)), rng.normal(size=(11, 2))) for _ in range(3)]
+    for f, (x, v) in enumerate(states, start=1):
+        w.submit(f, x, v)
+    w.flush()
+    w.close()
+    assert not os.path.exists(os.path.join(d, 'objs'))
+    for f, (x, v) in enumerate(states, start=1):
+        x2, v2 = frames.load_cache(frames.cache_path(d, f))
+        assert x2.shape == (11, 2) and np.array_equal(x2, x) and np.array_equal(v2, v)
+    with pytest.raises(ValueError):
+        frames.FrameWriter(d, None, 11, obj=True, dim=2)
