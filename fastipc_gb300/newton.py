@@ -307,6 +307,8 @@ class NewtonIPC:
         simulation stream); start_frame > 0 restarts from caches/{start_frame:06d}.p.  Returns
         the Newton iteration count of every step."""
         from . import frames
+        if start_frame > 0 and directory is None:
+            raise FastIPCError(5, 'a restart (start_frame > 0) reads caches/%06d.p from a directory')
         writer = None
         if directory is not None and (obj or cache):
             writer = frames.FrameWriter(directory, self.scene.boundary_triangles, self.nV, obj=obj, cache=cache)

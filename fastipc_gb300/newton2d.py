@@ -199,6 +199,8 @@ class NewtonIPC2D:
         The 2D write_image draws into a window and is not reproduced.  Returns the Newton
         iteration count of every step."""
         from . import frames
+        if start_frame > 0 and directory is None:
+            raise FastIPCError(5, 'a restart (start_frame > 0) reads caches/%06d.p from a directory')
         writer = frames.FrameWriter(directory, None, self.nV, obj=False, cache=True, dim=2) if directory is not None else None
         try:
             if start_frame > 0:
