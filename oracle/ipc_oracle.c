@@ -1491,3 +1491,292 @@ int oracle_bsr_pcg_guess(int nV, const long long* rp, const int* ci, const doubl
     free(r); free(z); free(p); free(Ap); free(Mi);
     return it;
 }
+
+/* ------------------------------------------------------------------------------------------
+ * 2D path (NEWTON_IPC.py with dim == 2), for the 2D oracle's fast mode and the CPU baseline.
+ * Methods differ from the GPU's: the 2x2 SVD comes from a Jacobi rotation of F^T F (the GPU
+ * uses the closed form of a scaled rotation plus reflection); the element Hessian is the
+ * reference's dP/dF mapped through the 4 x 6 derivative of F, as in the numpy oracle.
+ * ---------------------------------------------------------------------------------------- */
+
+/* F (row-major) = U diag(s) V^T with U, V rotations, s0 >= |s1|, s1 < 0 iff det F < 0 */
+static void svd2_jacobi(const double* F, double* U, double* s, double* V) {
+    const double a = F[0] * F[0] + F[2] * F[2], b = F[0] * F[1] + F[2] * F[3], d = F[1] * F[1] + F[3] * F[3];
+    const double th = 0.5 * atan2(2.0 * b, a - d);   /* rotation that diagonalises F^T F, larger first */
+    const double c = cos(th), sn = sin(th);
+    V[0] = c; V[1] = -sn; V[2] = sn; V[3] = c;       /* columns v0 = (c, sn), v1 = (-sn, c) */
+    const double f0x = F[0] * c + F[1] * sn, f0y = F[2] * c + F[3] * sn;          /* F v0 */
+    const double f1x = -F[0] * sn + F[1] * c, f1y = -F[2] * sn + F[3] * c;        /* F v1 */
+    double s0 = sqrt(f0x * f0x + f0y * f0y);
+    double ux = 1.0, uy = 0.0;
+    if (s0 > 0) { ux = f0x / s0; uy = f0y / s0; }
+    U[0] = ux; U[1] = -uy; U[2] = uy; U[3] = ux;     /* u1 = (-uy, ux) */
+    double s1 = -uy * f1x + ux * f1y;
+    if (fabs(s1) > s0) {                            /* the rotation picked the smaller value first */
+        /* swap the roles of v0 and v1 (v1 -> v0, -v0 -> v1 keeps V a rotation) */
+        V[0] = -sn; V[1] = -c; V[2] = c; V[3] = -sn;
+        const double g0x = f1x, g0y = f1y, g1x = -f0x, g1y = -f0y;
+        s0 = sqrt(g0x * g0x + g0y * g0y);
+        ux = 1.0; uy = 0.0;
+        if (s0 > 0) { ux = g0x / s0; uy = g0y / s0; }
+        U[0] = ux; U[1] = -uy; U[2] = uy; U[3] = ux;
+        s1 = -uy * g1x + ux * g1y;
+    }
+    s[0] = s0;
+    s[1] = s1;
+}
+
+/* fixed_corotated.py (dim 2): psi, P and the projected dPdF [j*2+i][s*2+r] */
+static double fc2_energy(const double* s, double la, double mu) {
+    const double a = s[0] - 1, b = s[1] - 1, p = s[0] * s[1] - 1;
+    return mu * (a * a + b * b) + la / 2 * p * p;
+}
+
+static void fc2_P_dPdF_oracle(const double* F, double la, double mu, double* P, double* dPdF, double* psi) {
+    double U[4], s[2], V[4];
+    svd2_jacobi(F, U, s, V);
+    *psi = fc2_energy(s, la, mu);
+    const double J = F[0] * F[3] - F[1] * F[2];
+    double R[4];
+    for (int i = 0; i < 2; ++i)
+        for (int k = 0; k < 2; ++k) R[2 * i + k] = U[2 * i] * V[2 * k] + U[2 * i + 1] * V[2 * k + 1];
+    const double cof[4] = {F[3], -F[2], -F[1], F[0]};
+    for (int k = 0; k < 4; ++k) P[k] = 2 * mu * (F[k] - R[k]) + la * (J - 1) * cof[k];
+    const double pm1 = s[0] * s[1] - 1;
+    const double g0 = 2 * mu * (s[0] - 1) + s[1] * la * pm1, g1 = 2 * mu * (s[1] - 1) + s[0] * la * pm1;
+    double Hs[4] = {2 * mu + la * s[1] * s[1], la * (pm1 + s[1] * s[0]), la * (pm1 + s[1] * s[0]), 2 * mu + la * s[0] * s[0]};
+    make_pd2(Hs);
+    const double left = mu - la / 2 * pm1;
+    const double sum = s[0] + s[1] > 0.000001 ? s[0] + s[1] : 0.000001;
+    const double right = (g0 + g1) / (2 * sum);
+    double B[4] = {left + right, left - right, left - right, left + right};
+    make_pd2(B);
+    double M[4][4];
+    memset(M, 0, sizeof(M));
+    M[0][0] = Hs[0]; M[0][3] = Hs[1]; M[3][0] = Hs[2]; M[3][3] = Hs[3];
+    M[1][1] = B[0]; M[1][2] = B[1]; M[2][1] = B[2]; M[2][2] = B[3];
+    /* the reference's eight-term sum: dPdF[ij][rs] = sum M[p][q] (u_a v_b^T)_ij (u_c v_d^T)_rs */
+    for (int j = 0; j < 2; ++j)
+        for (int i = 0; i < 2; ++i)
+            for (int ss = 0; ss < 2; ++ss)
+                for (int r = 0; r < 2; ++r) {
+                    double acc = 0;
+                    for (int p = 0; p < 4; ++p)
+                        for (int q = 0; q < 4; ++q) {
+                            if (M[p][q] == 0.0) continue;
+                            const int a = p / 2, b = p % 2, cc = q / 2, dd = q % 2;
+                            acc += M[p][q] * U[2 * i + a] * V[2 * j + b] * U[2 * r + cc] * V[2 * ss + dd];
+                        }
+                    dPdF[(j * 2 + i) * 4 + ss * 2 + r] = acc;
+                }
+}
+
+/* compute_elasticity for dim 2 (NEWTON_IPC.py:568-624): E [T], g [T][6], H [T][6][6] of
+ * dt^2 vol0 psi; IB [T][4] = restT^-1 row-major; any of E, g, H may be NULL */
+void oracle2d_elements(int nT, const int* tris, const double* x, const double* IB, const double* vol, const double* la,
+                       const double* mu, double dt, double* E, double* g, double* H) {
+    #pragma omp parallel for schedule(static)
+    for (int e = 0; e < nT; ++e) {
+        const double* X0 = x + 2 * tris[3 * e];
+        const double* X1 = x + 2 * tris[3 * e + 1];
+        const double* X2 = x + 2 * tris[3 * e + 2];
+        const double* ib = IB + 4 * e;
+        const double Ds[4] = {X1[0] - X0[0], X2[0] - X0[0], X1[1] - X0[1], X2[1] - X0[1]};
+        double F[4];
+        for (int i = 0; i < 2; ++i)
+            for (int k = 0; k < 2; ++k) F[2 * i + k] = Ds[2 * i] * ib[k] + Ds[2 * i + 1] * ib[2 + k];
+        double P[4], dPdF[16], psi;
+        fc2_P_dPdF_oracle(F, la[e], mu[e], P, dPdF, &psi);
+        const double w = dt * dt * vol[e];
+        if (E) E[e] = psi * w;
+        /* G[ij][2a+d] = delta_id D[a][j] */
+        const double D[3][2] = {{-ib[0] - ib[2], -ib[1] - ib[3]}, {ib[0], ib[1]}, {ib[2], ib[3]}};
+        double G[4][6];
+        memset(G, 0, sizeof(G));
+        for (int j = 0; j < 2; ++j)
+            for (int i = 0; i < 2; ++i)
+                for (int a = 0; a < 3; ++a) G[j * 2 + i][2 * a + i] = D[a][j];
+        if (g) {
+            const double Pv[4] = {P[0], P[2], P[1], P[3]};   /* vec index j*2+i of P_ij */
+            for (int n = 0; n < 6; ++n) {
+                double acc = 0;
+                for (int k = 0; k < 4; ++k) acc += Pv[k] * G[k][n];
+                g[6 * e + n] = acc * w;
+            }
+        }
+        if (H) {
+            double T[4][6];
+            for (int k = 0; k < 4; ++k)
+                for (int m = 0; m < 6; ++m) {
+                    double acc = 0;
+                    for (int l = 0; l < 4; ++l) acc += dPdF[k * 4 + l] * G[l][m];
+                    T[k][m] = acc;
+                }
+            for (int n = 0; n < 6; ++n)
+                for (int m = 0; m < 6; ++m) {
+                    double acc = 0;
+                    for (int k = 0; k < 4; ++k) acc += G[k][n] * T[k][m];
+                    H[36 * e + 6 * n + m] = acc * w;
+                }
+        }
+    }
+}
+
+static double pe2_d2(const double* p, const double* e0, const double* e1) {
+    const double ex = e1[0] - e0[0], ey = e1[1] - e0[1];
+    const double num = ey * p[0] - ex * p[1] + e1[0] * e0[1] - e1[1] * e0[0];
+    return num * num / (ex * ex + ey * ey);
+}
+static double pp2_d2(const double* a, const double* b) {
+    return (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]);
+}
+static int pe2_case(const double* p, const double* e0, const double* e1) {
+    const double ex = e1[0] - e0[0], ey = e1[1] - e0[1];
+    const double ratio = (ex * (p[0] - e0[0]) + ey * (p[1] - e0[1])) / (ex * ex + ey * ey);
+    return ratio < 0 ? 0 : (ratio > 1 ? 1 : 2);
+}
+
+/* find_constraints_2D_PE (NEWTON_IPC.py:159-179): candidate rows in any order (the caller
+ * sorts and de-duplicates them as np.unique does).  pp [cap][2], pe [cap][3]; returns the
+ * counts in n_out[2] (they may exceed cap: then the caller grows and calls again). */
+void oracle2d_find(int nBP, const int* bp, int nBE, const int* be, const double* x, double dhat2, int cap, int* pp, int* pe,
+                   int* n_out) {
+    const double dhat = sqrt(dhat2);
+    int npp = 0, npe = 0;
+    #pragma omp parallel for schedule(dynamic, 16)
+    for (int i = 0; i < nBP; ++i) {
+        const int p = bp[i];
+        const double* xp = x + 2 * p;
+        for (int j = 0; j < nBE; ++j) {
+            const int e0 = be[2 * j], e1 = be[2 * j + 1];
+            if (p == e0 || p == e1) continue;
+            const double* x0 = x + 2 * e0;
+            const double* x1 = x + 2 * e1;
+            int inside = 1;
+            for (int k = 0; k < 2; ++k) {
+                const double lo = fmin(x0[k], x1[k]), hi = fmax(x0[k], x1[k]);
+                if (!(xp[k] < hi + dhat && lo - dhat < xp[k])) inside = 0;
+            }
+            if (!inside) continue;
+            const int c = pe2_case(xp, x0, x1);
+            if (c < 2) {
+                const int o = c == 0 ? e0 : e1;
+                if (pp2_d2(xp, c == 0 ? x0 : x1) < dhat2) {
+                    int slot;
+                    #pragma omp atomic capture
+                    slot = npp++;
+                    if (slot < cap) { pp[2 * slot] = p < o ? p : o; pp[2 * slot + 1] = p < o ? o : p; }
+                }
+            } else if (pe2_d2(xp, x0, x1) < dhat2) {
+                int slot;
+                #pragma omp atomic capture
+                slot = npe++;
+                if (slot < cap) { pe[3 * slot] = p; pe[3 * slot + 1] = e0; pe[3 * slot + 2] = e1; }
+            }
+        }
+    }
+    n_out[0] = npp;
+    n_out[1] = npe;
+}
+
+/* point_edge_ccd with its broad phase (common/math/ipc.py:374-481), restated */
+static int pe2_overlap(const double* x0, const double* x1, const double* x2, const double* d0, const double* d1,
+                       const double* d2, double t) {
+    double p[2], a[2], b[2];
+    for (int k = 0; k < 2; ++k) { p[k] = x0[k] + d0[k] * t; a[k] = x1[k] + d1[k] * t; b[k] = x2[k] + d2[k] * t; }
+    const double ex = b[0] - a[0], ey = b[1] - a[1];
+    const double ratio = (ex * (p[0] - a[0]) + ey * (p[1] - a[1])) / (ex * ex + ey * ey);
+    return 0 <= ratio && ratio <= 1;
+}
+static double pe2_ccd_oracle(const double* x0, const double* x1, const double* x2, const double* d0, const double* d1,
+                             const double* d2, double eta) {
+    const int c = pe2_case(x0, x1, x2);
+    const double dist2 = c == 0 ? pp2_d2(x0, x1) : (c == 1 ? pp2_d2(x0, x2) : pe2_d2(x0, x1, x2));
+    const double m0 = d0[0] * d0[0] + d0[1] * d0[1], m1 = d1[0] * d1[0] + d1[1] * d1[1], m2 = d2[0] * d2[0] + d2[1] * d2[1];
+    const double mx = fmax(fmax(m0, m1), m2);
+    if (!(mx > 0)) return 1.0;
+    const double lb = (1 - eta) * sqrt(dist2) / (2 * sqrt(mx));
+    if (!(lb <= 1)) return 1.0;
+    const double A = d0[0] * (d2[1] - d1[1]) + d0[1] * (d1[0] - d2[0]) + d2[0] * d1[1] - d2[1] * d1[0];
+    const double Bq = x0[0] * (d2[1] - d1[1]) + d0[0] * (x2[1] - x1[1]) + d0[1] * (x1[0] - x2[0]) + x0[1] * (d1[0] - d2[0]) +
+                      d1[1] * x2[0] + d2[0] * x1[1] - d1[0] * x2[1] - d2[1] * x1[0];
+    const double C = x0[0] * (x2[1] - x1[1]) + x0[1] * (x1[0] - x2[0]) + x2[0] * x1[1] - x2[1] * x1[0];
+    double toc = 1.0, roots[2];
+    int nr = 0;
+    if (A == 0 && Bq == 0 && C == 0) {
+        const double* xe[2] = {x1, x2};
+        const double* de[2] = {d1, d2};
+        for (int k = 0; k < 2; ++k) {
+            const double rx = x0[0] - xe[k][0], ry = x0[1] - xe[k][1], vx = d0[0] - de[k][0], vy = d0[1] - de[k][1];
+            if (rx * vx + ry * vy < 0) {
+                const double t = sqrt((rx * rx + ry * ry) / (vx * vx + vy * vy));
+                if (t > 0 && t <= 1 && t * (1 - eta) < toc) toc = t * (1 - eta);
+            }
+        }
+    } else if (A == 0) {
+        if (Bq != 0) roots[nr++] = -C / Bq;
+    } else {
+        const double disc = Bq * Bq - 4 * A * C;
+        if (disc == 0) {
+            roots[nr++] = -Bq / (2 * A);
+        } else if (disc > 0) {
+            const double sq = sqrt(disc);
+            if (Bq > 0) { roots[nr++] = (-Bq - sq) / (2 * A); roots[nr++] = 2 * C / (-Bq - sq); }
+            else { roots[nr++] = 2 * C / (-Bq + sq); roots[nr++] = (-Bq + sq) / (2 * A); }
+        }
+    }
+    for (int k = 0; k < nr; ++k)
+        if (roots[k] > 0 && roots[k] <= 1 && pe2_overlap(x0, x1, x2, d0, d1, d2, roots[k]) && roots[k] * (1 - eta) < toc)
+            toc = roots[k] * (1 - eta);
+    return toc > lb ? toc : lb;
+}
+
+/* compute_filter_2D_PE (NEWTON_IPC.py:361-374): the smallest CCD step over all pairs */
+double oracle2d_ccd_step(int nBP, const int* bp, int nBE, const int* be, const double* x, const double* p, double dhat2,
+                         double eta) {
+    const double dhat = sqrt(dhat2);
+    double alpha = 1.0;
+    #pragma omp parallel for schedule(dynamic, 16) reduction(min:alpha)
+    for (int i = 0; i < nBP; ++i) {
+        const int q = bp[i];
+        const double* x0 = x + 2 * q;
+        const double* d0 = p + 2 * q;
+        for (int j = 0; j < nBE; ++j) {
+            const int a = be[2 * j], b = be[2 * j + 1];
+            if (q == a || q == b) continue;
+            const double *x1 = x + 2 * a, *x2 = x + 2 * b, *d1 = p + 2 * a, *d2 = p + 2 * b;
+            int ok = 1;
+            for (int k = 0; k < 2; ++k) {
+                const double lp = fmin(x0[k], x0[k] + d0[k]), hp = fmax(x0[k], x0[k] + d0[k]);
+                const double le = fmin(fmin(x1[k], x2[k]), fmin(x1[k] + d1[k], x2[k] + d2[k]));
+                const double he = fmax(fmax(x1[k], x2[k]), fmax(x1[k] + d1[k], x2[k] + d2[k]));
+                if (!(lp < he + dhat && le - dhat < hp)) ok = 0;
+            }
+            if (!ok) continue;
+            const double t = pe2_ccd_oracle(x0, x1, x2, d0, d1, d2, eta);
+            if (t < alpha) alpha = t;
+        }
+    }
+    return alpha;
+}
+
+/* check_collision_2D (NEWTON_IPC.py:843-854) with point_inside_triangle (ipc.py:502-509) */
+int oracle2d_collision(int nBP, const int* bp, int nT, const int* tris, const double* x) {
+    int hit = 0;
+    #pragma omp parallel for schedule(dynamic, 16) reduction(|:hit)
+    for (int i = 0; i < nBP; ++i) {
+        const int q = bp[i];
+        const double* P = x + 2 * q;
+        for (int e = 0; e < nT && !hit; ++e) {
+            const int a = tris[3 * e], b = tris[3 * e + 1], c = tris[3 * e + 2];
+            if (q == a || q == b || q == c) continue;
+            const double *A = x + 2 * a, *B = x + 2 * b, *C = x + 2 * c;
+            const double d1 = (P[0] - B[0]) * (A[1] - B[1]) - (P[1] - B[1]) * (A[0] - B[0]);
+            const double d2 = (P[0] - C[0]) * (B[1] - C[1]) - (P[1] - C[1]) * (B[0] - C[0]);
+            const double d3 = (P[0] - A[0]) * (C[1] - A[1]) - (P[1] - A[1]) * (C[0] - A[0]);
+            const int neg = d1 < 0 || d2 < 0 || d3 < 0, pos = d1 > 0 || d2 > 0 || d3 > 0;
+            if (!(neg && pos)) hit = 1;
+        }
+    }
+    return hit;
+}

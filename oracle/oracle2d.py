@@ -246,11 +246,53 @@ def check_collision(x, bp, tris):
     return False
 
 
+# ----------------------------------------------------------------------------- C (OpenMP) versions
+def elements_c(tris, x, IB, vol, la, mu, dt):
+    """elements() in the C oracle (ipc_oracle.c, oracle2d_elements): a Jacobi 2x2 SVD, OpenMP."""
+    tr = np.ascontiguousarray(tris, dtype=np.int32)
+    T = len(tr)
+    E, g, H = np.zeros(T), np.zeros((T, 6)), np.zeros((T, 6, 6))
+    O.lib().oracle2d_elements(T, O._p(tr, np.int32), O._p(O._f64(x)), O._p(O._f64(np.asarray(IB).reshape(T, 4))),
+                              O._p(O._f64(vol)), O._p(O._f64(la)), O._p(O._f64(mu)), O.D(dt), O._p(E), O._p(g), O._p(H))
+    return E, g, H
+
+
+def find_constraints_c(x, bp, be, dhat2):
+    """find_constraints() in the C oracle (candidate rows from OpenMP threads, then np.unique)."""
+    bp32, be32, xx = np.ascontiguousarray(bp, np.int32), np.ascontiguousarray(be, np.int32), O._f64(x)
+    cap = 1024
+    while True:
+        pp, pe, n = np.zeros((cap, 2), np.int32), np.zeros((cap, 3), np.int32), np.zeros(2, np.int32)
+        O.lib().oracle2d_find(len(bp32), O._p(bp32, np.int32), len(be32), O._p(be32, np.int32), O._p(xx), O.D(dhat2), cap,
+                              O._p(pp, np.int32), O._p(pe, np.int32), O._p(n, np.int32))
+        if n.max() <= cap:
+            break
+        cap = int(n.max()) * 2
+    return (np.unique(pp[:n[0]], axis=0).astype(np.int32).reshape(-1, 2),
+            np.unique(pe[:n[1]], axis=0).astype(np.int32).reshape(-1, 3))
+
+
+def ccd_step_c(x, p, bp, be, dhat2, eta=0.2):
+    bp32, be32 = np.ascontiguousarray(bp, np.int32), np.ascontiguousarray(be, np.int32)
+    L = O.lib()
+    L.oracle2d_ccd_step.restype = O.ctypes.c_double
+    return float(L.oracle2d_ccd_step(len(bp32), O._p(bp32, np.int32), len(be32), O._p(be32, np.int32), O._p(O._f64(x)),
+                                     O._p(O._f64(p)), O.D(dhat2), O.D(eta)))
+
+
+def check_collision_c(x, bp, tris):
+    bp32, tr = np.ascontiguousarray(bp, np.int32), np.ascontiguousarray(tris, np.int32)
+    return bool(O.lib().oracle2d_collision(len(bp32), O._p(bp32, np.int32), len(tr), O._p(tr, np.int32), O._p(O._f64(x))))
+
+
 # ----------------------------------------------------------------------------- driver
 class OracleSim2D:
-    """NEWTON_IPC.py with dim == 2, one instance per scene (fixed-corotated triangles)."""
+    """NEWTON_IPC.py with dim == 2, one instance per scene (fixed-corotated triangles).
+    fast=True runs the element, constraint, CCD and intersection loops in the C oracle (OpenMP
+    on all host cores) instead of numpy; the results agree to rounding."""
 
-    def __init__(self, scene):
+    def __init__(self, scene, fast=False):
+        self.fast = fast
         self.scene = scene
         self.dt, self.gravity = float(scene.dt), float(scene.gravity)
         self.dhat2 = float(scene.dhat) ** 2
@@ -288,14 +330,19 @@ class OracleSim2D:
         self.x[mask] = val[mask]
         self.xTilde[mask] = val[mask]
 
+    def _elements(self):
+        f = elements_c if self.fast else elements
+        return f(self.tris, self.x, self.IB, self.vol, self.la, self.mu, self.dt)
+
     def find_constraints(self):
-        self.PP, self.PE = find_constraints(self.x, self.bp, self.be, self.dhat2)
+        f = find_constraints_c if self.fast else find_constraints
+        self.PP, self.PE = f(self.x, self.bp, self.be, self.dhat2)
         return len(self.PP), len(self.PE)
 
     # NEWTON_IPC.py:514-542
     def compute_energy(self):
         e = 0.5 * np.sum(self.m * np.sum((self.x - self.xTilde) ** 2, 1))
-        e += np.sum(elements(self.tris, self.x, self.IB, self.vol, self.la, self.mu, self.dt)[0])
+        e += np.sum(self._elements()[0])
         for t, rows in ((0, self.PP), (1, self.PE)):
             if len(rows):
                 e += np.sum(barrier_rows(t, rows, self.x, self.dhat2, self.kappa)[0])
@@ -319,7 +366,7 @@ class OracleSim2D:
             cols.append(np.tile(d, (1, d.shape[1])).ravel())
             vals.append(H.reshape(len(idx), -1).ravel())
             np.add.at(rhs, d.ravel(), -g.ravel())
-        _, g, H = elements(self.tris, self.x, self.IB, self.vol, self.la, self.mu, self.dt)
+        _, g, H = self._elements()
         load(self.tris, g, H)
         for t, r in ((0, self.PP), (1, self.PE)):
             if len(r):
@@ -346,10 +393,12 @@ class OracleSim2D:
         return self.sol
 
     def compute_intersection_free_step_size(self):
-        return ccd_step(self.x, self.sol.reshape(-1, 2), self.bp, self.be, self.dhat2)
+        f = ccd_step_c if self.fast else ccd_step
+        return f(self.x, self.sol.reshape(-1, 2), self.bp, self.be, self.dhat2)
 
     def check_collision(self):
-        return check_collision(self.x, self.bp, self.tris)
+        f = check_collision_c if self.fast else check_collision
+        return f(self.x, self.bp, self.tris)
 
     def apply_sol(self, alpha):
         self.x = self.xPrev + self.sol.reshape(-1, 2) * alpha

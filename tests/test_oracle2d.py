@@ -149,3 +149,39 @@ def test_svd2_convention():
     assert np.all(np.linalg.det(U) > 0) and np.all(np.linalg.det(V) > 0)
     assert np.all(s[:, 0] >= np.abs(s[:, 1]))
     assert np.all((s[:, 1] < 0) == (np.linalg.det(F) < 0))
+
+
+def test_c_oracle_matches_numpy_oracle(newton2d_golden):
+    """The C (OpenMP) 2D loops against the numpy ones: elements (Jacobi against numpy SVD,
+    1e-11 relative), constraint lists (exact), CCD step and intersection flag, at the
+    reference's own iterates and at random deformations."""
+    g = newton2d_golden
+    sim = O2.OracleSim2D(golden_scene2d(g))
+    rng = np.random.default_rng(12)
+    states = [g[f'it{i}_x'] for i in (0, 5, 11)] + [g['x_rest'] + rng.normal(size=g['x_rest'].shape) * s for s in (1e-3, 8e-3)]
+    for x in states:
+        a = O2.elements(sim.tris, x, sim.IB, sim.vol, sim.la, sim.mu, sim.dt)
+        b = O2.elements_c(sim.tris, x, sim.IB, sim.vol, sim.la, sim.mu, sim.dt)
+        for u, v in zip(a, b):
+            assert np.abs(u - v).max() <= 1e-11 * max(np.abs(u).max(), 1e-300)
+        np.testing.assert_array_equal(O2.find_constraints(x, sim.bp, sim.be, sim.dhat2)[0],
+                                      O2.find_constraints_c(x, sim.bp, sim.be, sim.dhat2)[0])
+        np.testing.assert_array_equal(O2.find_constraints(x, sim.bp, sim.be, sim.dhat2)[1],
+                                      O2.find_constraints_c(x, sim.bp, sim.be, sim.dhat2)[1])
+        p = rng.normal(size=x.shape) * 2e-3
+        assert abs(O2.ccd_step(x, p, sim.bp, sim.be, sim.dhat2) - O2.ccd_step_c(x, p, sim.bp, sim.be, sim.dhat2)) <= 1e-12
+        assert O2.check_collision(x, sim.bp, sim.tris) == O2.check_collision_c(x, sim.bp, sim.tris)
+    x = g['x_rest'].copy()
+    x[len(x) // 2:-2, 1] -= 0.05
+    assert O2.check_collision_c(x, sim.bp, sim.tris) and O2.check_collision(x, sim.bp, sim.tris)
+
+
+def test_c_oracle_trajectory(newton2d_golden):
+    g = newton2d_golden
+    sim = O2.OracleSim2D(golden_scene2d(g), fast=True)
+    xs = []
+    for f in range(int(g['steps'])):
+        sim.step(f)
+        xs.append(sim.x.copy())
+    assert list(sim.newton_iters) == list(g['newton_iters'])
+    np.testing.assert_allclose(np.array(xs), g['x_steps'], atol=1e-6 * np.abs(g['x_init']).max(), rtol=0)
