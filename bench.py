@@ -74,10 +74,12 @@ def workload(args):
     if args.workload == 'lattice':
         return dict(common, workload='6x6x6 lattice of 0.1 m cubes (6 hexes per side x6 tets), seed-drawn rotations and +-10% '
                                      'jitter, dropped on a fixed 2x0.1x2 m ground box; NH E=1e5 nu=0.4, dhat=1e-3, dt=0.01',
-                    tets=279942, verts=74096)
+                    tets=279942, verts=74096, l2='inputs larger than L2 (element Hessians alone ~0.2 GB per Newton iteration)')
     if args.workload == 'cubes':
         return dict(common, workload='two 0.1 m cubes of 8x8x8 hexes x6 tets, upper one rotated (seed 0) and moving at -1 m/s; '
-                                     'NH E=1e5 nu=0.4, dhat=1e-3, dt=0.01', tets=6144, verts=1458)
+                                     'NH E=1e5 nu=0.4, dhat=1e-3, dt=0.01', tets=6144, verts=1458,
+                    l2='working set smaller than L2, not flushed between steps (a 6k-tet scene is bound by launches and '
+                       'host syncs, not by memory)')
     nx = args.nx
     return dict(common, workload=f'twisted bar {nx}x20x20 hexes x6 tets ({nx * 2400} tets), NH E=1e6 nu=0.45, dhat=5e-4, dt=0.01',
                 tets=nx * 2400, verts=(nx + 1) * 441, l2='inputs larger than L2 (element Hessians alone ~0.7 GB per Newton iteration)')
@@ -461,7 +463,8 @@ def main_2d(args):
     scene = SC.square_stack_2d(k=16, n=16, seed=0)
     cfg = {'workload': '2D: 16 squares of 16x16 quads x2 fixed-corotated triangles on a ground segment (4626 verts, '
                        '8192 tris), E=1e5 nu=0.4, dhat=1e-3, dt=0.01', 'tris': int(len(scene.tris)), 'verts': int(len(scene.x)),
-           'pcg_rtol': args.pcg_rtol, 'newton_tol': '|p|inf < 1e-2 dt', 'l2': 'working set below L2 (a 2D scene this size fits)'}
+           'pcg_rtol': args.pcg_rtol, 'newton_tol': '|p|inf < 1e-2 dt',
+           'l2': 'working set smaller than L2, not flushed between steps (the 2D step is bound by launch and barrier latency)'}
 
     def cpu_steps(x0, v0, f0, budget_s=20.0):
         from oracle import oracle2d as O2
