@@ -6,10 +6,12 @@
 // The reference tests every boundary point against every boundary edge (find_constraints_2D_PE,
 // compute_filter_2D_PE) and every boundary point against every triangle (check_collision_2D).
 // Here those all-pairs loops are tiled: a CTA stages a tile of edges (or triangles) with their
-// vertex positions in shared memory and every thread tests its point against the whole tile.
-// The system is assembled by sorting (block key, contribution id) pairs and summing each run in
-// id order, so every result is deterministic.  The direction comes from block-Jacobi PCG on
-// 2x2 blocks with fixed-order reductions.
+// vertex positions and FP32 boxes in shared memory and every thread tests its point against
+// the whole tile, the conservative FP32 box test first.  The system is assembled by sorting
+// (block key, contribution id) pairs and summing each run in id order, so every result is
+// deterministic.  The direction comes from block-Jacobi PCG on 2x2 blocks with fixed-order
+// reductions: one cooperative launch for systems that fit one CTA per SM, otherwise three
+// kernels per iteration replayed from a captured CUDA graph.
 #include <cuda_runtime.h>
 
 #include <string.h>
