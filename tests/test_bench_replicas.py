@@ -66,3 +66,14 @@ def test_reference_arm_under_torchrun_prints_one_line():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d['impl'] == 'reference' and d['value'] > 0 and d['n_gpus'] == 2
+
+
+def test_reference_arm_2d_prints_one_line():
+    """The 2D workload's reference arm (the 2D oracle on the host cores) prints one JSON line."""
+    cmd = [sys.executable, 'bench.py', '--impl', 'reference', '--workload', 'stack2d', '--steps', '1', '--warmup', '1']
+    r = subprocess.run(cmd, cwd=REPO, capture_output=True, text=True, timeout=600, env=dict(os.environ, OMP_NUM_THREADS='2'))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [l for l in r.stdout.splitlines() if l.startswith('{')]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d['impl'] == 'reference' and d['value'] > 0 and d['cpu_baseline']['cores'] == 2
