@@ -10,10 +10,15 @@
 // GPU that loads the library and stays allocated until the process exits.
 //
 // Set-up: the first call on a device (with that device current) looks up the array's device
-// address with cudaGetSymbolAddress and caches it for that device; make that first call before
-// any stream capture.  Every call on a device shares the one array and overwrites it, so calls
-// whose kernels overlap on the GPU (different streams, different host threads) race; order them
-// on one stream.
+// address with cudaGetSymbolAddress, caches it for that device, and loads this file's kernels
+// (under CUDA's lazy module loading a kernel's first launch would otherwise load it, and
+// loading can allocate device memory and synchronise).  So make that first call at start-up,
+// before the arena takes the device memory and before any stream capture; a call with zero
+// vertices, tets and rows does the set-up and writes 0.  The cached address does not survive
+// cudaDeviceReset: a process that resets a device must not call this entry point afterwards.
+// Every call on a device shares the one array and overwrites it, so calls whose kernels
+// overlap on the GPU (different streams, different host threads) race; order them on one
+// stream.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -36,7 +41,10 @@ namespace {
 std::mutex g_noalloc_mu;
 double* g_noalloc_addr[NOALLOC_MAX_DEVICES] = {nullptr};
 
-// device address of g_noalloc_partials for the current device (looked up once per device)
+int noalloc_load_kernels();
+
+// device address of g_noalloc_partials for the current device (looked up once per device,
+// which also loads this file's kernels on that device)
 int noalloc_scratch(double** out) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return FIPC_ERR_CUDA;
@@ -44,6 +52,8 @@ int noalloc_scratch(double** out) {
     if (!g_noalloc_addr[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_partials) != cudaSuccess || !p) return FIPC_ERR_CUDA;
+        const int st = noalloc_load_kernels();
+        if (st) return st;
         g_noalloc_addr[dev] = static_cast<double*>(p);
     }
     *out = g_noalloc_addr[dev];
@@ -123,6 +133,23 @@ __global__ void __launch_bounds__(NOALLOC_THREADS) k_na_sum(int total, const dou
     if (threadIdx.x == 0) *out = sh[0];
 }
 
+namespace {
+// cudaFuncGetAttributes loads a kernel on the current device, so the set-up call pays every
+// module load and later calls launch already-loaded kernels
+int noalloc_load_kernels() {
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, k_na_inertia) != cudaSuccess) return FIPC_ERR_CUDA;
+    if (cudaFuncGetAttributes(&a, k_na_elastic) != cudaSuccess) return FIPC_ERR_CUDA;
+    if (cudaFuncGetAttributes(&a, k_na_barrier) != cudaSuccess) return FIPC_ERR_CUDA;
+    if (cudaFuncGetAttributes(&a, k_na_sum) != cudaSuccess) return FIPC_ERR_CUDA;
+    return FIPC_OK;
+}
+
+// int4 row and tet loads need 16-byte alignment, double loads 8-byte
+inline bool al16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+inline bool al8(const void* p) { return ((uintptr_t)p & 7u) == 0; }
+}  // namespace
+
 }  // namespace fipc
 
 using namespace fipc;
@@ -143,8 +170,20 @@ int fipc_compute_energy_noalloc(int n_verts, const double* x, const double* xtil
     }
     if (blocks > NOALLOC_MAX_PARTIALS) return FIPC_ERR_CAPACITY;   // beyond the fixed scratch
     if (!energy || (n_verts && (!x || !xtilde || !mass)) || (n_tets && (!tets || !dm_inv || !vol || !lam || !mu))) return FIPC_ERR_ARGUMENT;
-    for (int t = 0; t < N_TYPES; ++t)
-        if (counts_h[t] > 0 && (!rows_h || !rows_h[t] || (t >= T_EEM && !x0))) return FIPC_ERR_ARGUMENT;
+    bool any_rows = false;
+    for (int t = 0; t < N_TYPES; ++t) {
+        if (counts_h[t] <= 0) continue;
+        any_rows = true;
+        if (!rows_h || !rows_h[t] || (t >= T_EEM && !x0)) return FIPC_ERR_ARGUMENT;
+        if (!al16(rows_h[t])) return FIPC_ERR_ARGUMENT;
+    }
+    // a misaligned vector load would raise a sticky CUDA error in the caller's context: refuse
+    // such pointers before anything is launched
+    if (!al8(energy)) return FIPC_ERR_ARGUMENT;
+    if ((n_verts || any_rows) && !al8(x)) return FIPC_ERR_ARGUMENT;
+    if (n_verts && (!al8(xtilde) || !al8(mass))) return FIPC_ERR_ARGUMENT;
+    if (n_tets && (!al16(tets) || !al8(x) || !al8(dm_inv) || !al8(vol) || !al8(lam) || !al8(mu))) return FIPC_ERR_ARGUMENT;
+    if (x0 && !al8(x0)) return FIPC_ERR_ARGUMENT;
     double* part = nullptr;
     const int st = noalloc_scratch(&part);
     if (st) return st;

@@ -126,11 +126,17 @@ int fipc_compute_energy(fipc_ctx* ctx, const double* x, const double* xtilde, do
  * cudaMalloc afterwards, since it synchronises the device and can fail against the arena).  No
  * counterpart in the reference.  Stateless: the caller passes mass [V], tets [T][4], dm_inv
  * [T][9], vol/lam/mu [T], counts_h [7] (host) and rows_h [7] (host array of device row
- * pointers), and receives the total in *energy (device).  The reduction's partial sums live in a
- * fixed file-scope device array of 65,536 doubles (512 KiB per GPU that loads the library, held
- * until exit): one partial per 256 vertices, tets or rows, so requests needing more (about 16.7M
- * elements in total) return status 1.  The first call on a device looks up that array and must
- * come before any stream capture; calls that overlap on the GPU share the array and race. */
+ * pointers), and receives the total in *energy (device).  It covers one scene with one kappa:
+ * for the concatenated scenes of a batch context (whose energy takes kappa per scene) it does
+ * not reproduce fipc_batch_compute_energy.  tets and every rows_h[t] with counts_h[t] > 0 must
+ * be 16-byte aligned and the double arrays 8-byte aligned (status 5 otherwise, before anything
+ * runs).  The reduction's partial sums live in a fixed file-scope device array of 65,536 doubles
+ * (512 KiB per GPU that loads the library, held until exit): one partial per 256 vertices, tets
+ * or rows, so requests needing more (about 16.7M elements in total) return status 1.  The first
+ * call on a device looks up that array and loads the kernels it launches, which can allocate
+ * and synchronise: make it at start-up, before the arena takes the memory and before any stream
+ * capture (a call with all sizes zero is enough).  The lookup is not redone after
+ * cudaDeviceReset.  Calls that overlap on the GPU share the array and race. */
 int fipc_compute_energy_noalloc(int n_verts, const double* x, const double* xtilde, const double* mass, int n_tets,
                                 const int* tets, const double* dm_inv, const double* vol, const double* lam,
                                 const double* mu, double dt, const int* counts_h, const int* const* rows_h,
