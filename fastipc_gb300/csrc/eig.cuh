@@ -14,12 +14,13 @@ namespace fipc {
 
 constexpr int EIG_LD = 9;  // row stride of the matrices handled here
 
-// a: n x n symmetric (row-major, stride EIG_LD).  On return a holds the orthonormal
+// a: n x n symmetric (row-major, stride LD, n <= LD).  On return a holds the orthonormal
 // eigenvectors in its columns and d the eigenvalues (ascending).  Returns 0 on success,
 // 1 if the QL iteration did not converge within its iteration limit.
-FIPC_HD int sym_eig(int n, double* a, double* d) {
-    double e[EIG_LD];
-#define A_(i, j) a[(i) * EIG_LD + (j)]
+template <int LD>
+FIPC_HD int sym_eig_ld(int n, double* a, double* d) {
+    double e[LD];
+#define A_(i, j) a[(i) * LD + (j)]
     // --- Householder tridiagonalisation, accumulating the orthogonal transform in a
     for (int i = n - 1; i > 0; --i) {
         const int l = i - 1;
@@ -142,22 +143,27 @@ FIPC_HD int sym_eig(int n, double* a, double* d) {
     return status;
 }
 
-// M (n x n, stride EIG_LD) <- its PSD projection; returns the sym_eig status.
-FIPC_HD int psd_project(int n, double* M) {
-    double Q[EIG_LD * EIG_LD], lam[EIG_LD];
+FIPC_HD int sym_eig(int n, double* a, double* d) { return sym_eig_ld<EIG_LD>(n, a, d); }
+
+// M (n x n, stride LD) <- its PSD projection; returns the sym_eig status.
+template <int LD>
+FIPC_HD int psd_project_ld(int n, double* M) {
+    double Q[LD * LD], lam[LD];
     for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) Q[i * EIG_LD + j] = M[i * EIG_LD + j];
-    const int st = sym_eig(n, Q, lam);
+        for (int j = 0; j < n; ++j) Q[i * LD + j] = M[i * LD + j];
+    const int st = sym_eig_ld<LD>(n, Q, lam);
     if (lam[0] >= 0.0) return st;
     for (int k = 0; k < n && lam[k] < 0.0; ++k) {
         const double l = lam[k];
         for (int i = 0; i < n; ++i) {
-            const double li = l * Q[i * EIG_LD + k];
-            for (int j = 0; j < n; ++j) M[i * EIG_LD + j] -= li * Q[j * EIG_LD + k];
+            const double li = l * Q[i * LD + k];
+            for (int j = 0; j < n; ++j) M[i * LD + j] -= li * Q[j * LD + k];
         }
     }
     return st;
 }
+
+FIPC_HD int psd_project(int n, double* M) { return psd_project_ld<EIG_LD>(n, M); }
 
 // 3x3 symmetric eigen-decomposition by cyclic Jacobi rotations (a: stride 3, destroyed;
 // v: eigenvectors in columns; w: eigenvalues, ascending).

@@ -8,6 +8,7 @@ from fastipc_gb300 import _native
 from fastipc_gb300.build import build
 
 HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), 'include', 'fastipc.h')
+ASO_HEADER = os.path.join(os.path.dirname(HEADER), 'fastipc_aso.h')
 
 
 def declared():
@@ -23,6 +24,16 @@ def test_header_matches_binding():
 def test_library_exports_all_symbols():
     lib = ctypes.CDLL(build())
     for name in declared():
+        assert hasattr(lib, name), name
+
+
+def test_library_exports_the_aso_functions():
+    """include/fastipc_aso.h: the scalar functions with the reference a.so's signatures."""
+    src = re.sub(r'/\*.*?\*/', '', open(ASO_HEADER).read(), flags=re.S)
+    names = sorted(set(re.findall(r'\bvoid\s+([a-z_0-9]+)\s*\(', src)))
+    assert len(names) == 17
+    lib = ctypes.CDLL(build())
+    for name in names:
         assert hasattr(lib, name), name
 
 
