@@ -8,10 +8,14 @@ A step is one implicit time step (the full Newton loop with CCD line search).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--nx 400]
 
 Ours: W warm-up steps, then K steps timed with CUDA events on the simulation stream between a
-barrier + synchronize on both sides (max over ranks); `value` = N*K / max time.  `e2e` re-runs
-the same K steps from the same state through the C-ABI path with the state copied from pinned
-host memory before each step and read back after it.  With --gpus N > 1 (torchrun) every rank
-runs an independent replica: the path has no data-parallel shard (one scene, one GPU).
+barrier + synchronize on both sides (max over ranks); `value` = N*K / max time.  Nothing inside
+the timed region records per-launch events.  `e2e` re-runs the same K steps from the same state
+through the C-ABI path with the state copied from pinned host memory before each step and read
+back after it.  The roofline comes from a separate instrumented pass over the same steps (CUDA
+events around every launch of the profiled kernel).  `trajectory` times the whole 200-step run of
+the scene from t = 0 and the CPU oracle on single steps taken from its states at steps 50, 100
+and 150.  With --gpus N > 1 (torchrun) every rank runs an independent replica: the path has no
+data-parallel shard (one scene, one GPU).
 
 Reference arm (--impl reference): the CPU oracle's implementation of the same Newton path
 (C/OpenMP kernels + block-Jacobi PCG, all host cores), timed on whole time steps of the same
@@ -23,7 +27,6 @@ import os
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -52,6 +55,10 @@ def parse():
     ap.add_argument('--learned-steps', type=int, default=20,
                     help='steps run from the timed state with the inertial and the learned start (0: skip)')
     ap.add_argument('--learned-weights', default=os.path.join(HERE, 'fastipc_gb300', 'weights', 'warmstart_bar400.npz'))
+    ap.add_argument('--trajectory', type=int, default=200,
+                    help='bar: time the whole run of this many steps from t = 0 beside the K-step window (0: skip)')
+    ap.add_argument('--cpu-samples', default='50,100,150',
+                    help='trajectory steps whose GPU states the CPU oracle steps once each (empty: none)')
     return ap.parse_args()
 
 
@@ -147,6 +154,46 @@ def ncu_traffic(kernel_id):
         return None, None
 
 
+def fp64_peak(dev):
+    """Measured FP64 FMA throughput of this GPU (TFLOP/s): the library's probe kernel (8
+    independent FMA chains per thread, 8 CTAs of 256 threads per SM), best of 5 launches timed
+    with CUDA events on the launching stream."""
+    import torch
+    from fastipc_gb300 import _native
+    L = _native.lib()
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    blocks, iters = 8 * nsm, 8192
+    out = torch.empty(blocks * 256, dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = _native.stream()
+
+    def launch():
+        _native.check(L.fipc_fp64_fma_probe(blocks, iters, _native.dptr(out), sp), 'fipc_fp64_fma_probe')
+    launch()
+    best = float('inf')
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        launch()
+        e1.record(stream)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    flops = blocks * 256 * iters * 16.0
+    return {'tflops': flops / (best / 1e3) / 1e12, 'ms': best, 'flops': flops,
+            'how': f'k_fp64_fma_probe: {blocks} CTAs x 256 threads x {iters} rounds x 8 FMA chains, best of 5 (CUDA events)'}
+
+
+def snapshot(sim):
+    return (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone(), {k: v.clone() for k, v in sim._dir_hist.items()})
+
+
+def restore(sim, snap):
+    sim.x.copy_(snap[0])
+    sim.v.copy_(snap[1])
+    sim.dx_prev.copy_(snap[2])
+    sim._dir_hist = {k: v.clone() for k, v in snap[3].items()}
+
+
 def cpu_baseline(scene, newton_per_step, pcg_per_newton, args):
     """The oracle on the host cores: one Newton iteration of time step 1 of the same scene
     (constraints, assembly, full PCG solve, line search), scaled to steps/s with the Newton and
@@ -176,12 +223,19 @@ def cpu_baseline(scene, newton_per_step, pcg_per_newton, args):
     t_pcg_it = (t2 - t1) / pcg_its
     t_newton = t_fixed + t_pcg_it * pcg_per_newton
     sps = 1.0 / (t_newton * newton_per_step)
+    t_own = t_fixed + t_pcg_it * pcg_its
     _ = E0
     return {'value': sps, 'unit': 'steps/s', 'cores': O.lib().oracle_num_threads(), 'kind': 'port',
             'sample': (f'one Newton iteration of step 1 of the same scene on the host cores ({t3 - t0:.1f} s: '
                        f'assembly+constraints+line search {t_fixed:.2f} s, PCG {pcg_its} its at {1e3 * t_pcg_it:.2f} ms/it); '
                        f'scaled by the timed GPU steps\' {newton_per_step:.2f} Newton its/step and {pcg_per_newton:.0f} PCG its/Newton'),
-            'ms_per_newton_iter': 1e3 * t_newton}
+            'ms_per_newton_iter': 1e3 * t_newton,
+            'matched_iterations': ('value: the CPU is credited with the GPU preconditioner\'s PCG iteration count '
+                                   '(the same algorithm on both sides)'),
+            'own_solver_value': 1.0 / (t_own * newton_per_step),
+            'own_solver': (f'the oracle\'s own block-Jacobi PCG ({pcg_its} its per Newton iteration in the sample), the '
+                           f'solver the reference arm (--impl reference) runs'),
+            'own_solver_ms_per_newton_iter': 1e3 * t_own}
 
 
 def max_over_ranks(ms, dist, device):
@@ -267,12 +321,11 @@ def main():
     for _ in range(args.warmup):
         sim.step(f)
         f += 1
-    snap = (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone())
-    hist = {k: v.clone() for k, v in sim._dir_hist.items()}
+    snap = snapshot(sim)
     f0 = f
     n_newton0, n_pcg0 = len(sim.newton_iters), len(sim.pcg_iters)
     L = _native.lib()
-    L.fipc_profile_enable(args.profile_kernel)
+    L.fipc_profile_enable(0)                  # no per-launch events inside the timed region
     stream = torch.cuda.current_stream(dev)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     launches0 = _native.launch_count()
@@ -286,8 +339,6 @@ def main():
         barrier()
     launches = _native.launch_count() - launches0
     ms = ev0.elapsed_time(ev1)
-    pt, pn, pb, pf = ctypes_read(L)
-    L.fipc_profile_enable(0)
     newton = sim.newton_iters[n_newton0:]
     pcg = sim.pcg_iters[n_pcg0:]
     ms_max = max_over_ranks(ms, dist, dev)
@@ -298,8 +349,7 @@ def main():
     hv = torch.empty_like(snap[1], device='cpu').pin_memory()
     hx.copy_(snap[0])
     hv.copy_(snap[1])
-    sim.newton_iters, sim.pcg_iters = [], []
-    sim._dir_hist = {k: v.clone() for k, v in hist.items()}
+    restore(sim, snap)
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -316,20 +366,47 @@ def main():
     e2e_ms = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     nbytes = 2 * sim.x.numel() * 8
 
+    # roofline: a separate instrumented pass over the first steps of the same window, with a CUDA
+    # event pair around every launch of the profiled kernel
+    restore(sim, snap)
+    n_prof = min(args.steps, 5)
+    barrier()
+    L.fipc_profile_enable(args.profile_kernel)
+    p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    for k in range(n_prof):
+        sim.step(f0 + k)
+    p1.record(stream)
+    barrier()
+    pt, pn, pb, pf = ctypes_read(L)
+    L.fipc_profile_enable(0)
+    prof_ms = p0.elapsed_time(p1)
+
     learned = learned_leg(sim, snap, f0, args) if args.learned_steps > 0 and args.workload == 'bar' else None
+    traj = trajectory_leg(sim, scene, args, dev) if args.trajectory > 0 and args.workload == 'bar' else None
 
     if rank == 0:
         pk, src = peaks()
+        fp64 = fp64_peak(dev)
         achieved = pb / (pt / 1e3) / 1e9 if pt > 0 else None
+        achieved_tf = pf / (pt / 1e3) / 1e12 if pt > 0 else None
         traffic, note = ncu_traffic(args.profile_kernel)
         newton_per_step = sum(newton) / len(newton)
         pcg_per_newton = sum(pcg) / max(len(pcg), 1)
-        roof = {'kernel': {1: 'k_pcg_spmv', 2: 'k_pcg_update', 3: 'k_elasticity'}.get(args.profile_kernel),
-                'bound': 'hbm', 'achieved': achieved, 'peak': pk['hbm_gbs'], 'unit': 'GB/s',
-                'frac': achieved / pk['hbm_gbs'] if achieved else None,
-                'traffic': traffic * 1.0 if traffic is not None else None,
-                'algorithmic_bytes_per_launch': pb / max(pn, 1), 'avg_launch_us': 1e3 * pt / max(pn, 1), 'launches': pn,
-                'peak_source': src, 'time_share_of_step': pt / ms if ms > 0 else None}
+        hbm = {'achieved': achieved, 'peak': pk['hbm_gbs'], 'unit': 'GB/s', 'frac': achieved / pk['hbm_gbs'] if achieved else None,
+               'peak_source': f'{src} (MEASURED_PEAKS.json hbm_gbs)' if src == 'measured' else 'fallback 6.8 TB/s'}
+        f64 = {'achieved': achieved_tf, 'peak': fp64['tflops'], 'unit': 'TFLOP/s',
+               'frac': achieved_tf / fp64['tflops'] if achieved_tf else None, 'peak_source': 'measured: ' + fp64['how']}
+        kname = {1: 'k_pcg_spmv', 2: 'k_pcg_update', 3: 'k_elasticity'}.get(args.profile_kernel)
+        # the binding unit of the profiled kernel, from its ncu capture: the FP64 pipe (SpMV 80%
+        # busy against 39% DRAM; update 62% against 21%; Neo-Hookean element 90% against 5%)
+        roof = {'kernel': kname, 'bound': 'fp64', 'achieved': achieved_tf, 'peak': fp64['tflops'], 'unit': 'TFLOP/s',
+                'frac': f64['frac'], 'traffic': traffic * 1.0 if traffic is not None else None,
+                'algorithmic_bytes_per_launch': pb / max(pn, 1), 'algorithmic_flops_per_launch': pf / max(pn, 1),
+                'avg_launch_us': 1e3 * pt / max(pn, 1), 'launches': pn, 'hbm': hbm, 'fp64': f64,
+                'binding': 'fp64 pipe (ncu: profiles/pcg_spmv_twisted_bar_960k.md)',
+                'measured_in': f'instrumented pass over steps {f0}..{f0 + n_prof - 1} after the timed region',
+                'time_share_of_step': pt / prof_ms if prof_ms > 0 else None}
         if note:
             roof['traffic_note'] = note
         out = {'metric': metric(args), 'value': value, 'unit': 'steps/s', 'n_gpus': world, 'steps': args.steps,
@@ -341,14 +418,89 @@ def main():
                        'd2h_bytes_per_step': nbytes},
                'gpu_launches': launches, 'roofline': roof, 'clocks': clk.summary(),
                'sections_s': {k: round(v, 4) for k, v in sim.timer.total.items()}}
+        if traj:
+            out['trajectory'] = traj
         if learned:
             out['learned_warm_start'] = learned
         if world == 1 and not args.no_cpu_baseline:
             out['cpu_baseline'] = cpu_baseline(scene, newton_per_step, pcg_per_newton, args)
+            if traj and traj.get('gpu_states') is not None:
+                traj.update(trajectory_cpu(scene, traj.pop('gpu_states'), args))
+        if traj:
+            traj.pop('gpu_states', None)
         print(json.dumps(out), flush=True)
     sim.close()
     if dist is not None:
         dist.destroy_process_group()
+
+
+def trajectory_leg(sim, scene, args, dev):
+    """The scene's whole run of args.trajectory steps from t = 0 (the initial state, an empty
+    PCG warm-start history), device-timed with one CUDA event per step; keeps the GPU states at
+    the --cpu-samples steps (device copies) for the CPU comparison."""
+    import torch
+    n = args.trajectory
+    samples = sorted({int(t) for t in args.cpu_samples.split(',') if t.strip() and 0 <= int(t) < n})
+    sim.set_state(scene.initial_positions(), scene.v)
+    sim.dx_prev.zero_()
+    sim._dir_hist = {}
+    stream = torch.cuda.current_stream(dev)
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(n + 1)]
+    states, newton, pcg = {}, [], []
+    torch.cuda.synchronize(dev)
+    evs[0].record(stream)
+    for f in range(n):
+        if f in samples:
+            states[f] = (sim.x.clone(), sim.v.clone())
+        p0 = len(sim.pcg_iters)
+        newton.append(sim.step(f))
+        pcg.append(sum(sim.pcg_iters[p0:]))
+        evs[f + 1].record(stream)
+    torch.cuda.synchronize(dev)
+    step_ms = [evs[f].elapsed_time(evs[f + 1]) for f in range(n)]
+    total = sum(step_ms)
+    out = {'steps': n, 'value': n / (total / 1e3), 'unit': 'steps/s', 'ms_per_step': total / n,
+           'newton_iters_per_step': sum(newton) / n, 'ms_per_newton_iter': total / max(sum(newton), 1),
+           'pcg_iters_per_newton': sum(pcg) / max(sum(newton), 1), 'how': 'device-timed (CUDA events), whole run from t = 0',
+           'per_quarter': []}
+    q = max(n // 4, 1)
+    for a in range(0, n, q):
+        b = min(a + q, n)
+        out['per_quarter'].append({'steps': f'{a}..{b - 1}', 'steps_per_s': (b - a) / (sum(step_ms[a:b]) / 1e3),
+                                   'newton_iters_per_step': sum(newton[a:b]) / (b - a)})
+    out['gpu_states'] = {f: (x.cpu().numpy(), v.cpu().numpy(), step_ms[f], newton[f], pcg[f]) for f, (x, v) in states.items()}
+    return out
+
+
+def trajectory_cpu(scene, states, args):
+    """The CPU oracle (all host cores, its own block-Jacobi PCG) takes one step from each of the
+    GPU's states, the same step the GPU took there; per-step rates on those steps, as measured
+    (own solver) and with the CPU credited with the GPU's PCG iteration count."""
+    from oracle import oracle as O
+    if not states:
+        return {}
+    sim = O.OracleSim(scene, solver='bsr', pcg_rtol=args.pcg_rtol, pcg_maxit=args.cpu_sample_pcg)
+    rows, g_ms, c_ms, c_ms_m = [], 0.0, 0.0, 0.0
+    for f in sorted(states):
+        x, v, gms, gnewton, gpcg = states[f]
+        sim.x, sim.v = x.copy(), v.copy()
+        sim.timings = {}
+        p0 = len(sim.pcg_iters)
+        t0 = time.perf_counter()
+        it = sim.step(f)
+        dt = time.perf_counter() - t0
+        cpcg = sum(sim.pcg_iters[p0:])
+        t_solve = sim.timings.get('Solve System', 0.0)
+        matched = dt - t_solve + (t_solve / max(cpcg, 1)) * gpcg
+        rows.append({'step': f, 'gpu_ms': gms, 'gpu_newton': gnewton, 'gpu_pcg': gpcg, 'cpu_ms': 1e3 * dt, 'cpu_newton': it,
+                     'cpu_pcg': cpcg, 'cpu_ms_matched_iterations': 1e3 * matched})
+        g_ms += gms
+        c_ms += 1e3 * dt
+        c_ms_m += 1e3 * matched
+    n = len(rows)
+    return {'cpu_samples': rows, 'cpu_cores': O.lib().oracle_num_threads(),
+            'gpu_steps_per_s_on_samples': n / (g_ms / 1e3), 'cpu_steps_per_s_on_samples': n / (c_ms / 1e3),
+            'cpu_steps_per_s_on_samples_matched_iterations': n / (c_ms_m / 1e3)}
 
 
 BATCH_METRIC = 'scene-steps/s (cube stacks, batched)'
@@ -585,9 +737,7 @@ def learned_leg(sim, snap, f0, args):
     if not os.path.exists(args.learned_weights):
         return {'unavailable': f'no weights at {os.path.relpath(args.learned_weights, HERE)}'}
     model = WarmStartMLP.load(args.learned_weights, device=sim.device)
-    sim.x.copy_(snap[0])
-    sim.v.copy_(snap[1])
-    sim.dx_prev.copy_(snap[2])
+    restore(sim, snap)
     warm = sim.pcg_warm_start
     sim.pcg_warm_start = False
     modes = {'plain': None, 'inertial': LearnedStart(kind='inertial'), 'learned': LearnedStart(model, kind='mlp', smooth=4)}

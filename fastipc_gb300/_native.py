@@ -21,7 +21,7 @@ EXPORTS = [
     'fipc_ctx_set_params', 'fipc_ctx_mass', 'fipc_ctx_set_x0', 'fipc_find_constraints', 'fipc_get_constraints',
     'fipc_compute_hessian_and_gradient', 'fipc_system_sizes', 'fipc_export_system', 'fipc_solve_system',
     'fipc_output_residual', 'fipc_compute_energy', 'fipc_compute_intersection_free_step_size', 'fipc_check_collision',
-    'fipc_launch_count', 'fipc_status_string', 'fipc_profile_enable', 'fipc_profile_read',
+    'fipc_launch_count', 'fipc_status_string', 'fipc_profile_enable', 'fipc_profile_read', 'fipc_fp64_fma_probe',
     'fipc_compute_energy_noalloc', 'fipc_mlp_param_count', 'fipc_mlp_forward', 'fipc_mlp_backward', 'fipc_mlp_mse',
     'fipc_mlp_adam', 'fipc_mlp_features', 'fipc_batch_create', 'fipc_batch_params', 'fipc_batch_compute_energy',
     'fipc_batch_output_residual', 'fipc_batch_step_size', 'fipc_batch_check_collision', 'fipc_batch_apply_sol',

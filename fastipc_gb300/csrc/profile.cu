@@ -30,6 +30,11 @@ cudaEvent_t get_event() {
 }
 }  // namespace
 
+int profile_kernel() {
+    std::lock_guard<std::mutex> lk(g_mu);
+    return g_kernel;
+}
+
 ProfScope::ProfScope(int kernel, cudaStream_t stream, double bytes_, double flops_) : id(kernel), s(stream), bytes(bytes_), flops(flops_) {
     std::lock_guard<std::mutex> lk(g_mu);
     if (g_kernel != id) return;
@@ -45,6 +50,26 @@ ProfScope::~ProfScope() {
     g_recs.push_back({a, b});
     g_bytes += bytes;
     g_flops += flops;
+}
+
+// FP64 throughput probe: 8 independent FMA chains per thread (enough independent work to fill
+// the FP64 pipe), iters rounds; every thread writes its sum so nothing is optimised away.
+// Flops per launch = blocks x 256 x iters x 16.
+__global__ void __launch_bounds__(256) k_fp64_fma_probe(int iters, double b, double c, double* __restrict__ out) {
+    const double s0 = 1e-9 * threadIdx.x;
+    double a0 = s0, a1 = s0 + 1e-3, a2 = s0 + 2e-3, a3 = s0 + 3e-3, a4 = s0 + 4e-3, a5 = s0 + 5e-3, a6 = s0 + 6e-3,
+           a7 = s0 + 7e-3;
+    for (int i = 0; i < iters; ++i) {
+        a0 = fma(a0, b, c);
+        a1 = fma(a1, b, c);
+        a2 = fma(a2, b, c);
+        a3 = fma(a3, b, c);
+        a4 = fma(a4, b, c);
+        a5 = fma(a5, b, c);
+        a6 = fma(a6, b, c);
+        a7 = fma(a7, b, c);
+    }
+    out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
 }
 
 }  // namespace fipc
@@ -81,6 +106,15 @@ int fipc_profile_read(double* total_ms, long long* launches, double* bytes, doub
     if (launches) *launches = (long long)g_recs.size();
     if (bytes) *bytes = g_bytes;
     if (flops) *flops = g_flops;
+    return FIPC_OK;
+}
+
+// one launch of the FP64 FMA probe: blocks x 256 threads, out [blocks * 256] (device)
+int fipc_fp64_fma_probe(int blocks, int iters, double* out, void* stream) {
+    if (blocks <= 0 || iters <= 0 || !out) return FIPC_ERR_ARGUMENT;
+    k_fp64_fma_probe<<<blocks, 256, 0, (cudaStream_t)stream>>>(iters, 0.999999, 1e-6, out);
+    FIPC_LAUNCHED();
+    FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
 }
 

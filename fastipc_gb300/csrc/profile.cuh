@@ -9,6 +9,9 @@ namespace fipc {
 
 enum ProfKernel : int { PK_NONE = 0, PK_PCG_SPMV = 1, PK_PCG_UPDATE = 2, PK_ELASTICITY = 3, PK_BARRIER = 4, PK_ASSEMBLE = 5 };
 
+// the kernel id being timed (PK_NONE when off)
+int profile_kernel();
+
 struct ProfScope {
     int id;
     cudaStream_t s;

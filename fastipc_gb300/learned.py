@@ -398,11 +398,22 @@ def collect_bar(nx, seed, steps, device='cuda:0', rest_relative=True, pcg_rtol=1
     return collect(sc, steps, device, pcg_rtol, rest_relative=rest_relative, stride=stride)
 
 
-def compare_starts(sim, steps, f0, modes, log=_log):
+def compare_starts(sim, steps, f0, modes, log=_log, warmup=1):
     """Run steps [f0, f0 + steps) from sim's current state once per mode (the state is restored
-    between modes).  modes: name -> None (plain) or a LearnedStart."""
+    between modes).  modes: name -> None (plain) or a LearnedStart.  Before the timed runs every
+    mode takes `warmup` untimed steps from the same state, so that first-use costs (buffer
+    growth for a large-motion CCD grid, the network's first launches) fall outside every mode's
+    wall time."""
     snap = (sim.x.clone(), sim.v.clone(), sim.dx_prev.clone())
     out, xs = {}, {}
+    for name, guess in modes.items():
+        sim.initial_guess = guess
+        for k in range(warmup):
+            if k == 0:
+                sim.x.copy_(snap[0])
+                sim.v.copy_(snap[1])
+                sim.dx_prev.copy_(snap[2])
+            sim.step(f0 + k)
     for name, guess in modes.items():
         sim.x.copy_(snap[0])
         sim.v.copy_(snap[1])

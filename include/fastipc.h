@@ -274,6 +274,10 @@ int fipc_write_obj(const char* path, int n_verts, const double* x_h, int n_tris,
  * milliseconds, launch count and the launches' algorithmic bytes and flops. */
 int fipc_profile_enable(int kernel_id);
 int fipc_profile_read(double* total_ms_h, long long* launches_h, double* bytes_h, double* flops_h);
+/* FP64 throughput probe for the FP64 roofline's denominator (no counterpart in the reference):
+ * one launch of blocks x 256 threads, each running 8 independent FMA chains for iters rounds
+ * (blocks x 256 x iters x 16 flops); out [blocks * 256] doubles (device) receives the sums. */
+int fipc_fp64_fma_probe(int blocks, int iters, double* out, void* stream);
 long long fipc_launch_count(void);           /* kernels launched by this library so far */
 const char* fipc_status_string(int status);
 
