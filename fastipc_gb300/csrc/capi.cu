@@ -67,6 +67,8 @@ double det3h(const double* A) {
 }
 
 void free_ctx(fipc_ctx* c) {
+    if (c->pcg3_exec) cudaGraphExecDestroy((cudaGraphExec_t)c->pcg3_exec);
+    c->pcg3_exec = nullptr;
     free_batch(c);
     cs_free(c);
     void* ptrs[] = {c->tets, c->bp, c->be, c->bt, c->dminv, c->vol, c->lam, c->mu, c->mass, c->x0, c->row_ptr, c->col_idx,
@@ -83,7 +85,7 @@ void free_ctx(fipc_ctx* c) {
     Grid* gs[] = {&c->gp, &c->ge};
     for (Grid* g : gs) {
         DBuf* gb[] = {&g->keys, &g->ids, &g->keys_alt, &g->ids_alt, &g->ukeys, &g->ustart, &g->counts, &g->offsets, &g->ncells, &g->tmp,
-                      &g->hkeys, &g->hvals};
+                      &g->hkeys, &g->hvals, &g->cell4, &g->box4};
         for (DBuf* b : gb) b->release();
     }
     delete c;
@@ -209,7 +211,8 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
                 }
                 const int u = (int)up_index[pos_of(i, j)];
                 which[10ull * e + b] = u;
-                contrib[10ull * e + b] = ((e * 10 + b) << 1) | tr;
+                // the block's place in the element kernel's tiled layout (32 tets per tile)
+                contrib[10ull * e + b] = ((((e >> 5) * 10 + b) * 32 + (e & 31)) << 1) | tr;
                 cnt[u + 1]++;
             }
         for (int u = 0; u < n_upper; ++u) cptr[u + 1] = cptr[u] + cnt[u + 1];
@@ -297,7 +300,7 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
     c->n_upper = n_upper;
     if (st == FIPC_OK) {
         if (cudaMalloc((void**)&c->elem_g, sizeof(double) * 12ull * (n_tets > 0 ? n_tets : 1)) != cudaSuccess ||
-            cudaMalloc((void**)&c->elem_H, sizeof(double) * 90ull * (n_tets > 0 ? n_tets : 1)) != cudaSuccess ||
+            cudaMalloc((void**)&c->elem_H, sizeof(double) * 2880ull * ((n_tets + 31) / 32 + 1)) != cudaSuccess ||
             cudaMalloc((void**)&c->bsr_val, sizeof(double) * 9ull * nnzb) != cudaSuccess ||
             cudaMalloc((void**)&c->sell_val, sizeof(double) * 288ull * (n_slots > 0 ? n_slots : 1)) != cudaSuccess ||
             cudaMemset(c->sell_val, 0, sizeof(double) * 288ull * (n_slots > 0 ? n_slots : 1)) != cudaSuccess ||

@@ -67,14 +67,37 @@ FIPC_HD int roots01(const double* op, int n, double* out) {
                 continue;
             }
             if (fb == 0.0 || (fa < 0.0) == (fb < 0.0)) continue;
+            // p is monotone on [a, b] (its ends are consecutive critical points), so the root is
+            // unique there: safeguarded Newton (p and p' by one Horner pass), the bracket
+            // shrinking at every step and a bisection step whenever Newton would leave it; stops
+            // once a step moves t by at most 1e-16 (the roots are interval ends in [0, 1]) or
+            // the bracket cannot be split further
+            double t = 0.5 * (a + b);
             for (int it = 0; it < 128; ++it) {
-                const double mid = 0.5 * (a + b);
-                if (mid <= a || mid >= b) break;
-                const double fm = horner(p, k, mid);
-                if (fm == 0.0) { a = b = mid; break; }
-                if ((fm < 0.0) == (fa < 0.0)) { a = mid; fa = fm; } else { b = mid; }
+                double f = p[0], df = 0.0;
+                for (int q = 1; q <= k; ++q) {
+                    df = df * t + f;
+                    f = f * t + p[q];
+                }
+                if (f == 0.0) {
+                    a = b = t;
+                    break;
+                }
+                if ((f < 0.0) == (fa < 0.0)) {
+                    a = t;
+                    fa = f;
+                } else {
+                    b = t;
+                }
+                double tn = df != 0.0 ? t - f / df : 0.5 * (a + b);
+                if (!(tn > a && tn < b)) tn = 0.5 * (a + b);
+                if (tn <= a || tn >= b || fabs(tn - t) <= 1e-16) {
+                    t = tn > a && tn < b ? tn : t;
+                    break;
+                }
+                t = tn;
             }
-            nx[m++] = 0.5 * (a + b);
+            nx[m++] = (a == b) ? a : t;
         }
         if (horner(p, k, 1.0) == 0.0 && (m == 0 || nx[m - 1] != 1.0)) nx[m++] = 1.0;
         nr = m;

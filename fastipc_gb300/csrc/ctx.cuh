@@ -54,6 +54,7 @@ struct DBuf {
 // unique keys and the start of each key's run
 struct Grid {
     DBuf keys, ids, keys_alt, ids_alt, ukeys, ustart, counts, offsets, ncells, tmp, hkeys, hvals;
+    DBuf cell4, box4;   // per stored primitive: first cell of its pair de-duplication, FP32 box
     int n_entries = 0, n_unique = 0;
     unsigned long long hmask = 0;   // cell table size - 1 (a power of two >= 2 x entries)
 };
@@ -124,6 +125,9 @@ struct fipc_ctx_impl {
     void* cap_stream = nullptr;           // private stream used only for capturing it
     std::vector<unsigned char> graph_sig; // the kernel arguments it was captured with
     float tune_ms = 0.f;                  // time of one SpMV launch in the chosen shape
+    // single-scene PCG: a captured chunk of iterations and the kernel arguments it holds
+    void* pcg3_exec = nullptr;
+    std::vector<unsigned char> pcg3_sig;
 };
 
 // scene lookup for the spatial hash: one scene (null table) or per-vertex scene ids with

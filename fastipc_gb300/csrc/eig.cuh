@@ -217,8 +217,15 @@ FIPC_HD void sym_eig3(double* a, double* w, double* v) {
     }
 }
 
-// 3x3 PSD projection (makePD for n = 3), stride 3
+// 3x3 PSD projection (makePD for n = 3), stride 3.  A matrix whose leading principal minors
+// are all positive (Sylvester's criterion) is positive definite and returned unchanged without
+// the eigen-solve, as makePD returns it when its smallest eigenvalue is >= 0.
 FIPC_HD void psd_project3(double* M) {
+    {
+        const double m1 = M[0], m2 = M[0] * M[4] - M[1] * M[3];
+        const double m3 = M[0] * (M[4] * M[8] - M[5] * M[7]) - M[1] * (M[3] * M[8] - M[5] * M[6]) + M[2] * (M[3] * M[7] - M[4] * M[6]);
+        if (m1 > 0.0 && m2 > 0.0 && m3 > 0.0) return;
+    }
     double a[9], w[3], v[9];
     for (int i = 0; i < 9; ++i) a[i] = M[i];
     sym_eig3(a, w, v);

@@ -14,26 +14,54 @@ namespace fipc {
 std::atomic<long long> g_launches{0};
 
 // ---------------------------------------------------------------- Neo-Hookean element
-// One thread per tet: gradient g[T,12] and the 10 upper Hessian blocks Hu[T,90] of
-// dt^2 vol0 psi(F) (NEWTON_IPC.py:568-691); energy E[T] when requested.
+// One thread per tet: gradient g[T,12] and the 10 upper Hessian blocks of dt^2 vol0 psi(F)
+// (NEWTON_IPC.py:568-691); energy E[T] when requested.  Hessian layouts:
+//  * TILED = false: Hu[T][90] (the stateless entry point's documented layout);
+//  * TILED = true (the context's assembly input): tiles of 32 consecutive tets, block b of tet
+//    e at Hu[((e / 32) * 10 + b) * 288 + (e % 32) * 9 + i], so each warp's block b is one
+//    contiguous 2,304-byte run, staged through shared memory and stored as full sectors (a
+//    per-thread 720-byte record written straight from registers reaches DRAM about twice).
+//    The buffer holds whole tiles.
+template <bool TILED>
 __global__ void __launch_bounds__(128) k_elasticity(int nT, const int4* __restrict__ tets, const double* __restrict__ x,
                                                     const double* __restrict__ dminv, const double* __restrict__ vol,
                                                     const double* __restrict__ lam, const double* __restrict__ mu, double dt2,
                                                     double* __restrict__ E, double* __restrict__ g, double* __restrict__ Hu) {
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= nT) return;
-    const int4 t = tets[e];
-    v3 X[4] = {ld3(x, t.x), ld3(x, t.y), ld3(x, t.z), ld3(x, t.w)};
-    double IB[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) IB[i] = dminv[9 * (size_t)e + i];
+    if (!TILED && e >= nT) return;
     double ge[12], He[90];
-    const double psi = nh_element(X, IB, lam[e], mu[e], dt2 * vol[e], ge, He);
-    if (E) E[e] = psi;
+    if (e < nT) {
+        const int4 t = tets[e];
+        v3 X[4] = {ld3(x, t.x), ld3(x, t.y), ld3(x, t.z), ld3(x, t.w)};
+        double IB[9];
 #pragma unroll
-    for (int i = 0; i < 12; ++i) g[12 * (size_t)e + i] = ge[i];
+        for (int i = 0; i < 9; ++i) IB[i] = dminv[9 * (size_t)e + i];
+        const double psi = nh_element(X, IB, lam[e], mu[e], dt2 * vol[e], ge, He);
+        if (E) E[e] = psi;
 #pragma unroll
-    for (int i = 0; i < 90; ++i) Hu[90 * (size_t)e + i] = He[i];
+        for (int i = 0; i < 12; ++i) g[12 * (size_t)e + i] = ge[i];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 90; ++i) He[i] = 0.0;
+    }
+    if (!TILED) {
+#pragma unroll
+        for (int i = 0; i < 90; ++i) Hu[90 * (size_t)e + i] = He[i];
+        return;
+    }
+    if ((e & ~31) >= nT) return;                   // a whole warp past the last tile
+    __shared__ double stage[4][32 * 9];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    double* tile = Hu + (size_t)(e >> 5) * 2880;   // the warp's 32 tets share e >> 5
+#pragma unroll
+    for (int b = 0; b < 10; ++b) {
+#pragma unroll
+        for (int i = 0; i < 9; ++i) stage[w][lane * 9 + i] = He[b * 9 + i];
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 9; ++k) tile[b * 288 + k * 32 + lane] = stage[w][k * 32 + lane];
+        __syncwarp();
+    }
 }
 
 // ---------------------------------------------------------------- barrier rows
@@ -274,12 +302,15 @@ __global__ void k_inversion_pairs(int n, const double* __restrict__ xs, const do
 static inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
 int launch_elasticity(int nT, const int* tets, const double* x, const double* dminv, const double* vol, const double* lam,
-                      const double* mu, double dt, double* E, double* g, double* Hu, cudaStream_t s) {
+                      const double* mu, double dt, double* E, double* g, double* Hu, cudaStream_t s, bool tiled) {
     if (nT <= 0) return FIPC_OK;
     {
         // per tet: 4 indices, 4 positions, Dm^-1, vol/lam/mu in; gradient and 10 blocks out
         ProfScope ps(PK_ELASTICITY, s, nT * (16.0 + 96.0 + 72.0 + 24.0 + 96.0 + 720.0 + (E ? 8.0 : 0.0)), 0.0);
-        k_elasticity<<<nblk(nT, 128), 128, 0, s>>>(nT, (const int4*)tets, x, dminv, vol, lam, mu, dt * dt, E, g, Hu);
+        if (tiled)
+            k_elasticity<true><<<nblk(nT, 128), 128, 0, s>>>(nT, (const int4*)tets, x, dminv, vol, lam, mu, dt * dt, E, g, Hu);
+        else
+            k_elasticity<false><<<nblk(nT, 128), 128, 0, s>>>(nT, (const int4*)tets, x, dminv, vol, lam, mu, dt * dt, E, g, Hu);
     }
     FIPC_LAUNCHED();
     FIPC_CUDA(cudaGetLastError());
@@ -336,7 +367,7 @@ extern "C" {
 int fipc_elasticity(int n_tets, const int* tets, const double* x, const double* dm_inv, const double* vol, const double* lam,
                     const double* mu, double dt, double* E, double* g, double* Hu, void* stream) {
     if (n_tets < 0 || !tets || !x || !dm_inv || !vol || !lam || !mu || !g || !Hu) return FIPC_ERR_ARGUMENT;
-    return launch_elasticity(n_tets, tets, x, dm_inv, vol, lam, mu, dt, E, g, Hu, (cudaStream_t)stream);
+    return launch_elasticity(n_tets, tets, x, dm_inv, vol, lam, mu, dt, E, g, Hu, (cudaStream_t)stream, false);
 }
 
 int fipc_barrier_rows(int type, int n_rows, const int* rows, const double* x, const double* x0, double dhat2, double kappa,

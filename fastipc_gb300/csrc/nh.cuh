@@ -161,23 +161,23 @@ FIPC_HD double nh_element(const v3* X, const double* IB, double la, double mu, d
     }
     // sigma-space gradient / projected Hessian and the three 2x2 blocks (neo_hookean.py:75-98)
     const double lp = log(s[0] * s[1] * s[2]);
+    const double inv[3] = {1.0 / s[0], 1.0 / s[1], 1.0 / s[2]};
     double gs[3], Hs[9];
     for (int i = 0; i < 3; ++i) {
-        const double inv = 1.0 / s[i];
-        gs[i] = mu * (s[i] - inv) + la * inv * lp;
-        const double i2 = 1.0 / s[i] / s[i];
+        gs[i] = mu * (s[i] - inv[i]) + la * inv[i] * lp;
+        const double i2 = inv[i] * inv[i];
         Hs[i * 4] = mu * (1.0 + i2) - la * i2 * (lp - 1.0);
     }
-    Hs[1] = Hs[3] = la / s[0] / s[1];
-    Hs[5] = Hs[7] = la / s[1] / s[2];
-    Hs[2] = Hs[6] = la / s[0] / s[2];
+    Hs[1] = Hs[3] = la * inv[0] * inv[1];
+    Hs[5] = Hs[7] = la * inv[1] * inv[2];
+    Hs[2] = Hs[6] = la * inv[0] * inv[2];
     psd_project3(Hs);
     const double middle = mu - la * lp;
     double Bk[3][4];
     const int pa[3] = {0, 1, 2}, pb[3] = {1, 2, 0};
     for (int k = 0; k < 3; ++k) {
         const int i = pa[k], j = pb[k];
-        const double left = (mu + middle / s[i] / s[j]) / 2.0;
+        const double left = (mu + middle * inv[i] * inv[j]) / 2.0;
         double right = gs[i] + gs[j];
         const double ss = fmax(s[i] + s[j], 0.000001);
         right /= (2 * ss);
@@ -185,8 +185,14 @@ FIPC_HD double nh_element(const v3* X, const double* IB, double la, double mu, d
         Bk[k][1] = left - right;
         Bk[k][2] = left - right;
         Bk[k][3] = left + right;
-        make_pd2(Bk[k]);
+        // its eigenvalues are 2 left and 2 right: with both clearly positive make_pd leaves the
+        // block unchanged, so its square root is skipped
+        if (!(left > 1e-8 * fabs(right) && right > 1e-8 * fabs(left))) make_pd2(Bk[k]);
     }
+    // the weight dt^2 vol0 folded into the sigma-space coefficients once
+    for (int i = 0; i < 9; ++i) Hs[i] *= wgt;
+    for (int k = 0; k < 3; ++k)
+        for (int i = 0; i < 4; ++i) Bk[k][i] *= wgt;
     // z_b over the 4 vertices
     double z[3][4];
     for (int b = 0; b < 3; ++b) {
@@ -198,9 +204,14 @@ FIPC_HD double nh_element(const v3* X, const double* IB, double la, double mu, d
         }
         z[b][0] = -acc;
     }
-    int blk = 0;
-    for (int v = 0; v < 4; ++v)
-        for (int w = v; w < 4; ++w, ++blk) {
+    // Blocks (v, w) with 1 <= v <= w <= 3 directly: U C U^T with C built from z_b[v] z_d[w].  The
+    // Hessian is bilinear in (z[.][v], z[.][w]) and z[.][0] = -(z[.][1] + z[.][2] + z[.][3]), so
+    // the blocks of vertex 0 follow by sums: H(0,w) = -sum_{v>=1} H(v,w) with H(v,w) = H(w,v)^T,
+    // and H(0,0) = -sum_{w>=1} H(0,w)^T.
+#pragma unroll
+    for (int v = 1; v < 4; ++v)
+#pragma unroll
+        for (int w = v; w < 4; ++w) {
             double Z[3][3];  // Z[b][d] = z_b[v] z_d[w]
             for (int b = 0; b < 3; ++b)
                 for (int d = 0; d < 3; ++d) Z[b][d] = z[b][v] * z[d][w];
@@ -215,13 +226,33 @@ FIPC_HD double nh_element(const v3* X, const double* IB, double la, double mu, d
             C[2 * 3 + 1] = Hs[7] * Z[2][1] + Bk[1][2] * Z[1][2];
             C[0 * 3 + 2] = Hs[2] * Z[0][2] + Bk[2][2] * Z[2][0];
             C[2 * 3 + 0] = Hs[6] * Z[2][0] + Bk[2][1] * Z[0][2];
-            // block = w * U C U^T
             double T[9];
             for (int i = 0; i < 3; ++i)
                 for (int c = 0; c < 3; ++c) T[i * 3 + c] = U[i * 3 + 0] * C[0 * 3 + c] + U[i * 3 + 1] * C[1 * 3 + c] + U[i * 3 + 2] * C[2 * 3 + c];
+            // Hu block of (v, w), v <= w: (1,1) 4, (1,2) 5, (1,3) 6, (2,2) 7, (2,3) 8, (3,3) 9
+            double* out = Hu + 9 * (v == 1 ? 3 + w : (v == 2 ? 5 + w : 9));
             for (int i = 0; i < 3; ++i)
                 for (int j = 0; j < 3; ++j)
-                    Hu[blk * 9 + i * 3 + j] = wgt * (T[i * 3 + 0] * U[j * 3 + 0] + T[i * 3 + 1] * U[j * 3 + 1] + T[i * 3 + 2] * U[j * 3 + 2]);
+                    out[i * 3 + j] = T[i * 3 + 0] * U[j * 3 + 0] + T[i * 3 + 1] * U[j * 3 + 1] + T[i * 3 + 2] * U[j * 3 + 2];
+        }
+    // H(0,w), w = 1..3 (blocks 1..3) and H(0,0) (block 0)
+    const double* H11 = Hu + 36;
+    const double* H12 = Hu + 45;
+    const double* H13 = Hu + 54;
+    const double* H22 = Hu + 63;
+    const double* H23 = Hu + 72;
+    const double* H33 = Hu + 81;
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const int ij = i * 3 + j, ji = j * 3 + i;
+            Hu[9 + ij] = -(H11[ij] + H12[ji] + H13[ji]);
+            Hu[18 + ij] = -(H12[ij] + H22[ij] + H23[ji]);
+            Hu[27 + ij] = -(H13[ij] + H23[ij] + H33[ij]);
+        }
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            const int ji = j * 3 + i;
+            Hu[i * 3 + j] = -(Hu[9 + ji] + Hu[18 + ji] + Hu[27 + ji]);
         }
     return psi;
 }

@@ -14,6 +14,8 @@
 // (the reference's DBC_set_zeros + identity, NEWTON_IPC.py:756-772).  Per iteration an SpMV and
 // an update kernel on a fixed grid (plus the two coarse kernels); dot products are per-block
 // partials summed in a fixed order by the last block, so results are bitwise reproducible.
+#include <algorithm>
+
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
@@ -29,7 +31,8 @@ __device__ __forceinline__ double* sell_block(double* val, int enc) {
 }
 
 // one thread per upper block: fixed-order sum of its contributions, written to (i,j) and
-// transposed to (j,i) in the sliced-ELL value array (entry stride 32)
+// transposed to (j,i) in the sliced-ELL value array (entry stride 32).  A contribution is
+// (position of its 3x3 block in the tiled element-Hessian array / 9) << 1 | transposed.
 __global__ void k_assemble_elastic(int n_upper, const int* __restrict__ cptr, const int* __restrict__ contrib,
                                    const int* __restrict__ spos, const int* __restrict__ tspos, const int* __restrict__ urow,
                                    const double* __restrict__ elem_H, const double* __restrict__ mass, double* __restrict__ val) {
@@ -265,11 +268,13 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const doub
         a.flag[0] = (t == 0.0 || t <= rtol * rtol * tt[1]) ? 1 : 0;
         a.flag[1] = 0;
         a.flag[2] = 0;
+        a.flag[3] = 0;
     }
 }
 
-// iteration k, part 1: w = A u and the dot products; the last block derives alpha, beta
-__global__ void __launch_bounds__(PCG_THREADS) k_pcg_spmv(PCGArgs a, int k) {
+// iteration k (= flag[3], kept on the device so that a captured chunk of iterations replays
+// unchanged), part 1: w = A u and the dot products; the last block derives alpha, beta
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_spmv(PCGArgs a) {
     if (*(volatile int*)&a.flag[0]) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double g = 0.0, dl = 0.0, rr = 0.0;
@@ -291,12 +296,14 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_spmv(PCGArgs a, int k) {
         final_sums<3>(a, tt);
         if (threadIdx.x != 0) return;
         const double G = tt[0], Dl = tt[1], R = tt[2];
+        const int k = a.flag[3];
         a.flag[2] = 0;
         if (R <= a.sc[SC_TOL2]) {
             a.flag[0] = 1;
             a.flag[1] = k;
             return;
         }
+        a.flag[3] = k + 1;
         const double beta = k == 0 ? 0.0 : G / a.sc[SC_GAMMA];
         const double alpha = k == 0 ? G / Dl : G / (Dl - beta * G / a.sc[SC_ALPHA]);
         a.sc[SC_GAMMA] = G;
@@ -366,7 +373,7 @@ static int cub_call(fipc_ctx* c, F&& f) {
 }
 
 int launch_elasticity(int nT, const int* tets, const double* x, const double* dminv, const double* vol, const double* lam,
-                      const double* mu, double dt, double* E, double* g, double* Hu, cudaStream_t s);
+                      const double* mu, double dt, double* E, double* g, double* Hu, cudaStream_t s, bool tiled);
 int launch_barrier_rows(int type, int n, const int* rows, const double* x, const double* x0, double dh2, double kappa,
                         const double* kap_s, const int* vscene, double* E, double* g, double* Hb, int* status, cudaStream_t s);
 
@@ -378,7 +385,7 @@ void cs_apply(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s);
 int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t s) {
     int st = cs_offsets(c, x, s);
     if (st) return st;
-    st = launch_elasticity(c->nT, c->tets, x, c->dminv, c->vol, c->lam, c->mu, c->dt, nullptr, c->elem_g, c->elem_H, s);
+    st = launch_elasticity(c->nT, c->tets, x, c->dminv, c->vol, c->lam, c->mu, c->dt, nullptr, c->elem_g, c->elem_H, s, true);
     if (st) return st;
     k_assemble_elastic<<<nblk(c->n_upper, 128), 128, 0, s>>>(c->n_upper, c->up_cptr, c->up_contrib, c->up_spos, c->up_tspos,
                                                              c->up_row, c->elem_H, c->mass, c->sell_val);
@@ -463,6 +470,52 @@ int sell_to_bsr(fipc_ctx* c, double* out, cudaStream_t s) {
     return FIPC_OK;
 }
 
+// iterations per captured graph of the single-scene PCG: iterations after convergence return at
+// their first instruction, so a chunk overshoots by at most PCG3_CHUNK - 1 empty launches
+constexpr int PCG3_CHUNK = 32;
+
+// a graph of PCG3_CHUNK iterations (SpMV, update, coarse correction) for these kernel
+// arguments, captured on the context's private stream and replayed on the caller's; reused
+// while the arguments (buffers, sizes) stay the same; false when capture is unavailable
+static bool pcg3_graph(fipc_ctx* c, const PCGArgs& a) {
+    const unsigned char* sig = reinterpret_cast<const unsigned char*>(&a);
+    if (c->pcg3_exec && c->pcg3_sig.size() == sizeof(PCGArgs) && std::equal(sig, sig + sizeof(PCGArgs), c->pcg3_sig.begin()))
+        return true;
+    if (c->pcg3_exec) cudaGraphExecDestroy((cudaGraphExec_t)c->pcg3_exec);
+    c->pcg3_exec = nullptr;
+    c->pcg3_sig.clear();
+    if (!c->cap_stream) {
+        cudaStream_t cs;
+        if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return false;
+        c->cap_stream = cs;
+    }
+    cudaStream_t cs = (cudaStream_t)c->cap_stream;
+    const int nb = nblk(c->nV, PCG_THREADS);
+    const long long counted = g_launches.load();   // captured launches run (and count) at replay
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
+    for (int k = 0; k < PCG3_CHUNK; ++k) {
+        k_pcg_spmv<<<nb, PCG_THREADS, 0, cs>>>(a);
+        k_pcg_update<<<nb, PCG_THREADS, 0, cs>>>(a);
+        if (a.cs_blocks) cs_apply(c, a, cs);
+    }
+    g_launches.store(counted);
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(cs, &g) != cudaSuccess || !g) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaGraphExec_t ex = nullptr;
+    const bool ok = cudaGraphInstantiate(&ex, g, 0ull) == cudaSuccess;
+    cudaGraphDestroy(g);
+    if (!ok) {
+        cudaGetLastError();
+        return false;
+    }
+    c->pcg3_exec = ex;
+    c->pcg3_sig.assign(sig, sig + sizeof(PCGArgs));
+    return true;
+}
+
 // solve_system (NEWTON_IPC.py:750-777) by block-Jacobi PCG; sol: device [3 nV] holding the
 // initial guess on entry (zero for the reference's semantics) and the solution on return
 int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, double rtol, int maxit, double* sol, int* iters,
@@ -496,7 +549,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     a.part = c->pcg_part.as<double>();
     a.sc = a.part + 3 * nb;
     a.flag = (int*)(c->scal.as<char>() + 48);
-    FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 3 * sizeof(int), s));
+    FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 4 * sizeof(int), s));
     int st = cs_prepare(c, fixed, a, s);
     if (st) return st;
     // traffic model per launch: matrix blocks and column ids once (padding slots included),
@@ -510,20 +563,34 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     FIPC_LAUNCHED();
     if (a.cs_blocks) cs_apply(c, a, s);
     int h_flag[2] = {0, 0};
-    const int chunk = 64;
-    for (int k0 = 0; k0 < maxit; k0 += chunk) {
-        for (int k = k0; k < k0 + chunk && k < maxit; ++k) {
-            {
-                ProfScope ps(PK_PCG_SPMV, s, spmv_bytes, spmv_flops);
-                k_pcg_spmv<<<nb, PCG_THREADS, 0, s>>>(a, k);
+    // per-launch timing of the SpMV or the update needs plain launches; otherwise whole chunks of
+    // iterations replay from a captured graph (one launch per chunk instead of four per iteration)
+    const int pk = profile_kernel();
+    const bool timed = pk == PK_PCG_SPMV || pk == PK_PCG_UPDATE;
+    const bool graph = !timed && maxit >= PCG3_CHUNK && pcg3_graph(c, a);
+    const int per_iter = a.cs_blocks ? 4 : 2;
+    int k0 = 0;
+    while (k0 < maxit) {
+        if (graph && k0 + PCG3_CHUNK <= maxit) {
+            FIPC_CUDA(cudaGraphLaunch((cudaGraphExec_t)c->pcg3_exec, s));
+            g_launches.fetch_add(PCG3_CHUNK * per_iter, std::memory_order_relaxed);
+            k0 += PCG3_CHUNK;
+        } else {
+            const int k1 = (k0 + PCG3_CHUNK < maxit) ? k0 + PCG3_CHUNK : maxit;
+            for (int k = k0; k < k1; ++k) {
+                {
+                    ProfScope ps(PK_PCG_SPMV, s, spmv_bytes, spmv_flops);
+                    k_pcg_spmv<<<nb, PCG_THREADS, 0, s>>>(a);
+                }
+                FIPC_LAUNCHED();
+                {
+                    ProfScope ps(PK_PCG_UPDATE, s, upd_bytes, upd_flops);
+                    k_pcg_update<<<nb, PCG_THREADS, 0, s>>>(a);
+                }
+                FIPC_LAUNCHED();
+                if (a.cs_blocks) cs_apply(c, a, s);
             }
-            FIPC_LAUNCHED();
-            {
-                ProfScope ps(PK_PCG_UPDATE, s, upd_bytes, upd_flops);
-                k_pcg_update<<<nb, PCG_THREADS, 0, s>>>(a);
-            }
-            FIPC_LAUNCHED();
-            if (a.cs_blocks) cs_apply(c, a, s);
+            k0 = k1;
         }
         FIPC_CUDA(cudaMemcpyAsync(h_flag, a.flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
         FIPC_CUDA(cudaStreamSynchronize(s));

@@ -200,3 +200,29 @@ def test_ccd_vs_reference_so(so, ref, unit_golden):
             for xq, pq, dd in zip(xs, g[f'ccd_{name}_p'], d2):
                 a, b = o(*xq.ravel(), *(scale * pq).ravel(), 0.2, dd)[0], r(*xq.ravel(), *(scale * pq).ravel(), 0.2, dd)[0]
                 assert abs(a - b) < 1e-6
+
+
+def test_ccd_random_near_contact_vs_reference_so(so, ref):
+    """2000 seeded point-triangle and edge-edge pairs a few millimetres apart, moving towards,
+    past and along each other: the exports against the reference's a.so within 1e-6."""
+    rng = np.random.default_rng(11)
+    for kind in (0, 1):
+        fn = 'point_triangle_ccd' if kind == 0 else 'edge_edge_ccd'
+        o, r = bind(so, fn, 26, 1), bind(ref, fn, 26, 1)
+        xs, ps = [], []
+        for _ in range(2000):
+            base = rng.normal(size=(4, 3)) * 0.01
+            if kind == 0:
+                base[0] = base[1:].mean(axis=0) + rng.normal(size=3) * 0.003
+            else:
+                base[2:] = base[:2].mean(axis=0) + rng.normal(size=(2, 3)) * 0.006
+            xs.append(base)
+            ps.append(rng.normal(size=(4, 3)) * rng.choice([0.001, 0.005, 0.02]))
+        xs = np.array(xs)
+        d2 = _dist2(kind, xs)
+        hits = 0
+        for xq, pq, dd in zip(xs, ps, d2):
+            a, b = o(*xq.ravel(), *pq.ravel(), 0.2, dd)[0], r(*xq.ravel(), *pq.ravel(), 0.2, dd)[0]
+            assert abs(a - b) < 1e-6, (kind, a, b)
+            hits += b < 1.0
+        assert hits > 100
