@@ -170,7 +170,8 @@ FIPC_HD double helmert(int nv, int v, int a) {
 // Energy (E), gradient (g, 12 = 3*nv used) and projected Hessian in 3x3 vertex blocks
 // (Hb[(v*4+w)*9 + i*3+j] for v,w < nv) of one constraint row.  X: the row's vertices
 // (nv used), X0: rest positions of the four EE-type vertices (mollified types only).
-// want: 0 energy only, 1 energy + gradient + Hessian.  Returns the eigen-solver status.
+// want: 0 energy only, 1 energy + gradient + projected Hessian, 2 energy + gradient + the
+// Hessian without the projection.  Returns the eigen-solver status.
 FIPC_HD int barrier_row(int type, const v3* X, const v3* X0, double dh2, double kappa, int want,
                         double* E, double* g, double* Hb) {
     const RowMap m = row_map(type);
@@ -248,7 +249,9 @@ FIPC_HD int barrier_row(int type, const v3* X, const v3* X0, double dh2, double 
                     M[(3 * a + i) * 9 + 3 * bb + j] = s;
                 }
     int st = 0;
-    if (n == 3) {
+    if (want == 2) {
+        // no projection
+    } else if (n == 3) {
         double M3[9];
         for (int i = 0; i < 3; ++i)
             for (int j = 0; j < 3; ++j) M3[i * 3 + j] = M[i * 9 + j];

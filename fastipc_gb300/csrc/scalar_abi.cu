@@ -18,6 +18,7 @@
 
 #include "../../include/fastipc_aso.h"
 #include "ccd.cuh"
+#include "ldlt.cuh"
 #include "eig.cuh"
 #include "fc2d.cuh"
 #include "nh.cuh"
@@ -25,8 +26,6 @@
 namespace {
 
 using namespace fipc;
-
-constexpr int PD_LD = 12;
 
 // n x n row-major symmetric `in` -> its PSD projection in `out` (the makePD rule of
 // common/math/wrapper/UTILS.h:8-25: unchanged when the smallest eigenvalue is >= 0, otherwise
@@ -49,106 +48,6 @@ void project_pd_n(int n, const double* in, double* const* out) {
                 if (lam[k] > 0.0) s += lam[k] * Q[i * PD_LD + k] * Q[j * PD_LD + k];
             *out[i * n + j] = s;
         }
-}
-
-// In-place LDL^T with symmetric diagonal pivoting on a (n x n, stride PD_LD, lower triangle
-// read): step k brings to position k the remaining row whose ORIGINAL diagonal entry has the
-// largest magnitude (the first of equal ones), the pivot order of the reference's Eigen LDLT
-// (its choice looks at the input's diagonal, not at the updated Schur complement).  perm[k] =
-// the row swapped with k at step k.  On return the strict lower triangle holds L (unit
-// diagonal) and the diagonal holds D, both in the permuted order.  A zero pivot leaves its
-// column of L at zero.
-void ldlt_pivoted(int n, double* a, int* perm) {
-#define A_(i, j) a[(i) * PD_LD + (j)]
-    double dg[PD_LD];
-    for (int i = 0; i < n; ++i) {
-        dg[i] = A_(i, i);
-        for (int j = i + 1; j < n; ++j) A_(i, j) = A_(j, i);   // keep a full symmetric copy
-    }
-    for (int k = 0; k < n; ++k) {
-        int p = k;
-        for (int i = k + 1; i < n; ++i)
-            if (fabs(dg[i]) > fabs(dg[p])) p = i;
-        perm[k] = p;
-        if (p != k) {
-            const double t = dg[k];
-            dg[k] = dg[p];
-            dg[p] = t;
-            for (int j = 0; j < n; ++j) {
-                const double u = A_(k, j);
-                A_(k, j) = A_(p, j);
-                A_(p, j) = u;
-            }
-            for (int i = 0; i < n; ++i) {
-                const double u = A_(i, k);
-                A_(i, k) = A_(i, p);
-                A_(i, p) = u;
-            }
-        }
-        const double d = A_(k, k);
-        if (d == 0.0) {
-            for (int i = k + 1; i < n; ++i) A_(i, k) = A_(k, i) = 0.0;
-            continue;
-        }
-        for (int i = k + 1; i < n; ++i) {
-            const double lik = A_(i, k) / d;
-            for (int j = k + 1; j <= i; ++j) A_(i, j) -= lik * A_(j, k);
-            for (int j = k + 1; j <= i; ++j) A_(j, i) = A_(i, j);
-        }
-        for (int i = k + 1; i < n; ++i) {
-            A_(i, k) /= d;
-            A_(k, i) = A_(i, k);
-        }
-    }
-#undef A_
-}
-
-// x = A^+ b from the factorisation above (pseudo-inverse of D: zero pivots give zero)
-void ldlt_solve(int n, const double* f, const int* perm, const double* b, double* x) {
-    double y[PD_LD];
-    for (int i = 0; i < n; ++i) y[i] = b[i];
-    for (int k = 0; k < n; ++k)
-        if (perm[k] != k) {
-            const double t = y[k];
-            y[k] = y[perm[k]];
-            y[perm[k]] = t;
-        }
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < i; ++j) y[i] -= f[i * PD_LD + j] * y[j];
-    for (int i = 0; i < n; ++i) y[i] = f[i * PD_LD + i] != 0.0 ? y[i] / f[i * PD_LD + i] : 0.0;
-    for (int i = n - 1; i >= 0; --i)
-        for (int j = i + 1; j < n; ++j) y[i] -= f[j * PD_LD + i] * y[j];
-    for (int k = n - 1; k >= 0; --k)
-        if (perm[k] != k) {
-            const double t = y[k];
-            y[k] = y[perm[k]];
-            y[perm[k]] = t;
-        }
-    for (int i = 0; i < n; ++i) x[i] = y[i];
-}
-
-// solve_N of wrapper.cpp:90-198: factor A = P^T L D L^T P, raise every pivot of D to at least
-// 1e-8, rebuild F = L D L^T (in the pivoted order, as the reference rebuilds it from the factors
-// alone) and solve F x = rhs.  When no pivoting happens F is A with its pivots clamped.
-void solve_n(int n, const double* in, const double* rhs, double* const* out) {
-    double a[PD_LD * PD_LD], f[PD_LD * PD_LD], x[PD_LD];
-    int perm[PD_LD];
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j < n; ++j) a[i * PD_LD + j] = in[i * n + j];
-    ldlt_pivoted(n, a, perm);
-    for (int i = 0; i < n; ++i)
-        for (int j = 0; j <= i; ++j) {
-            double s = 0.0;
-            for (int k = 0; k <= j; ++k) {
-                const double lik = k == i ? 1.0 : a[i * PD_LD + k];
-                const double ljk = k == j ? 1.0 : a[j * PD_LD + k];
-                s += lik * fmax(a[k * PD_LD + k], 1e-8) * ljk;
-            }
-            f[i * PD_LD + j] = f[j * PD_LD + i] = s;
-        }
-    ldlt_pivoted(n, f, perm);
-    ldlt_solve(n, f, perm, rhs, x);
-    for (int i = 0; i < n; ++i) *out[i] = x[i];
 }
 
 // 2x2 SVD in the convention of the reference's svd_2 (JGSL, wrapper.cpp:12-25): F = R S with R
@@ -402,7 +301,9 @@ void solve_2(double in_0, double in_1, double in_2, double in_3, double rhs_0, d
     const double in[4] = {in_0, in_1, in_2, in_3};
     const double rhs[2] = {rhs_0, rhs_1};
     double* const out[2] = {out_0, out_1};
-    solve_n(2, in, rhs, out);
+    double x[2];
+    solve_n(2, in, rhs, x);
+    for (int i = 0; i < 2; ++i) *out[i] = x[i];
 }
 
 void solve_3(double in_0, double in_1, double in_2, double in_3, double in_4, double in_5, double in_6, double in_7,
@@ -410,7 +311,9 @@ void solve_3(double in_0, double in_1, double in_2, double in_3, double in_4, do
     const double in[9] = {in_0, in_1, in_2, in_3, in_4, in_5, in_6, in_7, in_8};
     const double rhs[3] = {rhs_0, rhs_1, rhs_2};
     double* const out[3] = {out_0, out_1, out_2};
-    solve_n(3, in, rhs, out);
+    double x[3];
+    solve_n(3, in, rhs, x);
+    for (int i = 0; i < 3; ++i) *out[i] = x[i];
 }
 
 void solve_4(double in_0, double in_1, double in_2, double in_3, double in_4, double in_5, double in_6, double in_7,
@@ -421,7 +324,9 @@ void solve_4(double in_0, double in_1, double in_2, double in_3, double in_4, do
                          in_14, in_15};
     const double rhs[4] = {rhs_0, rhs_1, rhs_2, rhs_3};
     double* const out[4] = {out_0, out_1, out_2, out_3};
-    solve_n(4, in, rhs, out);
+    double x[4];
+    solve_n(4, in, rhs, x);
+    for (int i = 0; i < 4; ++i) *out[i] = x[i];
 }
 
 void solve_6(double in_0, double in_1, double in_2, double in_3, double in_4, double in_5, double in_6, double in_7,
@@ -436,7 +341,9 @@ void solve_6(double in_0, double in_1, double in_2, double in_3, double in_4, do
                          in_27, in_28, in_29, in_30, in_31, in_32, in_33, in_34, in_35};
     const double rhs[6] = {rhs_0, rhs_1, rhs_2, rhs_3, rhs_4, rhs_5};
     double* const out[6] = {out_0, out_1, out_2, out_3, out_4, out_5};
-    solve_n(6, in, rhs, out);
+    double x[6];
+    solve_n(6, in, rhs, x);
+    for (int i = 0; i < 6; ++i) *out[i] = x[i];
 }
 
 void solve_9(double in_0, double in_1, double in_2, double in_3, double in_4, double in_5, double in_6, double in_7,
@@ -462,7 +369,9 @@ void solve_9(double in_0, double in_1, double in_2, double in_3, double in_4, do
                          in_79, in_80};
     const double rhs[9] = {rhs_0, rhs_1, rhs_2, rhs_3, rhs_4, rhs_5, rhs_6, rhs_7, rhs_8};
     double* const out[9] = {out_0, out_1, out_2, out_3, out_4, out_5, out_6, out_7, out_8};
-    solve_n(9, in, rhs, out);
+    double x[9];
+    solve_n(9, in, rhs, x);
+    for (int i = 0; i < 9; ++i) *out[i] = x[i];
 }
 // ---- wrapper.cpp:200-252 ------------------------------------------------------------------
 void get_smallest_positive_real_quad_root(double a, double b, double c, double tol, double* ret) {
