@@ -11,6 +11,7 @@
 // every pair is tested once without a hash set.  The narrow phase applies the reference's exact
 // predicates; constraint rows are then sorted lexicographically and de-duplicated per list
 // exactly like np.unique(axis=0) (NEWTON_IPC.py:348-356).
+#include <cooperative_groups.h>
 #include <cub/cub.cuh>
 #include <cuda_runtime.h>
 
@@ -19,6 +20,8 @@
 #include "geometry.cuh"
 
 namespace fipc {
+
+namespace cg = cooperative_groups;
 
 struct C3 {
     long long x, y, z;
@@ -114,6 +117,62 @@ __global__ void k_cell_emit(int mode, int n, const int* __restrict__ prim, const
             }
 }
 
+// Candidate records of the stored primitives, built with the grid, so that the query kernels
+// reject most candidates without FP64 work (GB300 issues FP64 at a small fraction of its FP32
+// rate):
+//  * cell: cell_of(stored lower corner), the first-cell test of the queries' pair
+//    de-duplication, computed with the same FP64 expression;
+//  * box: an FP32 box rounded outward around the FP64 box that the query's own FP64 test
+//    compares against: mode 0 the point; 1 and 3 the (moving) edge box +- dh (ee_aabb,
+//    ee_aabb_moving); 2 the moving point's box (pt_aabb_moving); 4 the edge box +- dh (the
+//    intersection check, whose segment-triangle test cannot hit a triangle whose box is dh
+//    away).  A candidate whose FP32 box misses the query's FP32 box (also rounded outward)
+//    fails the FP64 test too, so the lists, steps and flags are unchanged.
+__device__ __forceinline__ float4 f32_lo(v3 a) {
+    return make_float4(__double2float_rd(a.x), __double2float_rd(a.y), __double2float_rd(a.z), 0.f);
+}
+__device__ __forceinline__ float4 f32_hi(v3 a) {
+    return make_float4(__double2float_ru(a.x), __double2float_ru(a.y), __double2float_ru(a.z), 0.f);
+}
+__device__ __forceinline__ bool f32_overlap(float4 alo, float4 ahi, float4 blo, float4 bhi) {
+    return alo.x < bhi.x && alo.y < bhi.y && alo.z < bhi.z && blo.x < ahi.x && blo.y < ahi.y && blo.z < ahi.z;
+}
+__device__ __forceinline__ int clamp_cell(long long c) {
+    return (int)(c < -(1ll << 30) ? -(1ll << 30) : (c > (1ll << 30) ? (1ll << 30) : c));
+}
+
+__global__ void k_cand_records(int mode, int n, const int* __restrict__ prim, const double* __restrict__ x,
+                               const double* __restrict__ p, double dh, SceneGeo g, int4* __restrict__ cell,
+                               float4* __restrict__ box) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double inv_dx = g.idx(g.scene(prim_vertex(mode, i, prim)));
+    v3 lo, hi;
+    stored_box(mode, i, prim, x, p, dh, &lo, &hi);
+    const C3 c = cell_of(lo, inv_dx);
+    cell[i] = make_int4(clamp_cell(c.x), clamp_cell(c.y), clamp_cell(c.z), 0);
+    const v3 d = mk(dh, dh, dh);
+    v3 blo = lo, bhi = hi;
+    if (mode == 0) {                      // the point itself
+        blo = ld3(x, prim[i]);
+        bhi = blo;
+    } else if (mode == 2) {               // the moving point's box, without dh
+        const v3 a = ld3(x, prim[i]), b = a + ld3(p, prim[i]);
+        blo = vmin(a, b);
+        bhi = vmax(a, b);
+    } else if (mode == 1 || mode == 3) {  // edge box +- dh, as ee_aabb(_moving) forms it
+        blo = lo - d;
+        bhi = hi + d;
+    }
+    box[2 * (size_t)i] = f32_lo(blo);
+    box[2 * (size_t)i + 1] = f32_hi(bhi);
+}
+
+struct CandView {
+    const int4* cell;
+    const float4* box;
+};
+
 // Cell lookup of a built grid: an open-addressing table (linear probing, load factor <= 1/2)
 // maps each occupied cell key to its run of ids, so a query cell costs one or two probes instead
 // of a binary search over all keys.  The table holds exactly the sorted grid's runs; which slot a
@@ -175,8 +234,17 @@ struct RowSink {
     int* counts;   // [N_TYPES + 1]; the last entry is the overflow flag
     int cap;
 };
+// Warp-aggregated emission: the lanes that reach this call together are partitioned by target
+// list; one lane of each partition reserves the partition's rows with a single atomicAdd and
+// every lane writes its row at base + its rank.  The lists are sorted and de-duplicated
+// afterwards, so the order of the rows within a list does not matter.
 __device__ __forceinline__ void emit(const RowSink& s, int t, int a, int b, int c, int d) {
-    const int k = atomicAdd(&s.counts[t], 1);
+    const cg::coalesced_group active = cg::coalesced_threads();
+    const cg::coalesced_group same = cg::labeled_partition(active, t);
+    int base = 0;
+    if (same.thread_rank() == 0) base = atomicAdd(&s.counts[t], (int)same.size());
+    base = same.shfl(base, 0);
+    const int k = base + (int)same.thread_rank();
     if (k < s.cap) s.rows[t][k] = make_int4(a, b, c, d);
     else atomicOr(&s.counts[N_TYPES], 1);
 }
@@ -236,7 +304,7 @@ __device__ void attempt_ee(const double* __restrict__ x, const double* __restric
 // one thread per boundary triangle; points hashed with mode 0
 __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
                                                  const double* __restrict__ x, double dh, double dh2, SceneGeo g,
-                                                 GridView gv, RowSink sink) {
+                                                 GridView gv, CandView cv, RowSink sink) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     if (g.big_tri && g.big_tri[i]) return;
@@ -244,7 +312,10 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
     const int sc = g.scene(t0);
     const double inv_dx = g.idx(sc);
     const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
-    const C3 lo = cell_of(vmin(vmin(A, B), C), inv_dx), hi = cell_of(vmax(vmax(A, B), C), inv_dx);
+    const v3 tmn = vmin(vmin(A, B), C), tmx = vmax(vmax(A, B), C);
+    const C3 lo = cell_of(tmn, inv_dx), hi = cell_of(tmx, inv_dx);
+    const v3 d = mk(dh, dh, dh);
+    const float4 qlo = f32_lo(tmn - d), qhi = f32_hi(tmx + d);   // pt_aabb's triangle box
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
@@ -252,10 +323,11 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
                 if (c < 0) continue;
                 for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
                     const int j = gv.ids[k];
-                    const int p = bp[j];
-                    const C3 plo = cell_of(ld3(x, p) - mk(dh, dh, dh), inv_dx);
-                    const C3 first = cmax(lo, plo);
+                    const int4 pc = __ldg(cv.cell + j);
+                    const C3 first = cmax(lo, C3{pc.x, pc.y, pc.z});
                     if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (!f32_overlap(__ldg(cv.box + 2 * j), __ldg(cv.box + 2 * j + 1), qlo, qhi)) continue;
+                    const int p = bp[j];
                     attempt_pt(x, dh, dh2, p, t0, t1, t2, sink);
                 }
             }
@@ -264,7 +336,7 @@ __global__ void __launch_bounds__(128) k_find_pt(int nbt, const int* __restrict_
 // one thread per boundary edge (query, box +- dh); stored edges hashed with mode 1
 __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
                                                  const double* __restrict__ x0, double dh, double dh2, SceneGeo g,
-                                                 GridView gv, RowSink sink) {
+                                                 GridView gv, CandView cv, RowSink sink) {
     // QG lanes per query edge share the candidates of each cell
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
     if (i >= nbe) return;
@@ -275,6 +347,7 @@ __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict_
     const v3 A0 = ld3(x, a0), A1 = ld3(x, a1);
     const v3 d = mk(dh, dh, dh);
     const C3 lo = cell_of(vmin(A0, A1) - d, inv_dx), hi = cell_of(vmax(A0, A1) + d, inv_dx);
+    const float4 qlo = f32_lo(vmin(A0, A1)), qhi = f32_hi(vmax(A0, A1));   // ee_aabb's query edge box
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
@@ -283,10 +356,11 @@ __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict_
                 for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
                     const int j = gv.ids[k];
                     if (!(i < j)) continue;
-                    const int b0 = be[2 * j], b1 = be[2 * j + 1];
-                    const C3 slo = cell_of(vmin(ld3(x, b0), ld3(x, b1)), inv_dx);
-                    const C3 first = cmax(lo, slo);
+                    const int4 sc4 = __ldg(cv.cell + j);
+                    const C3 first = cmax(lo, C3{sc4.x, sc4.y, sc4.z});
                     if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (!f32_overlap(__ldg(cv.box + 2 * j), __ldg(cv.box + 2 * j + 1), qlo, qhi)) continue;
+                    const int b0 = be[2 * j], b1 = be[2 * j + 1];
                     attempt_ee(x, x0, dh, dh2, a0, a1, b0, b1, sink);
                 }
             }
@@ -300,7 +374,7 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* slot, double 
 // compute_filter_3D_PT (NEWTON_IPC.py:377-406): triangles query their moving bbox
 __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
                                                 const double* __restrict__ x, const double* __restrict__ p, double dh, SceneGeo g,
-                                                double eta, GridView gv, unsigned long long* __restrict__ alpha) {
+                                                double eta, GridView gv, CandView cv, unsigned long long* __restrict__ alpha) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     if (g.big_tri && g.big_tri[i]) return;
@@ -313,18 +387,21 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
     const v3 mx = vmax(vmax(vmax(A, A + dA), vmax(B, B + dB)), vmax(C, C + dC));
     const C3 lo = cell_of(mn, inv_dx), hi = cell_of(mx, inv_dx);
     const v3 d = mk(dh, dh, dh);
+    const float4 qlo = f32_lo(mn - d), qhi = f32_hi(mx + d);   // pt_aabb_moving's triangle box
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
                 const int c = gv.find(gkey(g, sc, cx, cy, cz));
                 if (c < 0) continue;
                 for (int k = gv.us[c]; k < gv.us[c + 1]; ++k) {
-                    const int pp = bp[gv.ids[k]];
+                    const int j = gv.ids[k];
+                    const int4 pc = __ldg(cv.cell + j);
+                    const C3 first = cmax(lo, C3{pc.x, pc.y, pc.z});
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (!f32_overlap(__ldg(cv.box + 2 * j), __ldg(cv.box + 2 * j + 1), qlo, qhi)) continue;
+                    const int pp = bp[j];
                     if (pp == t0 || pp == t1 || pp == t2) continue;
                     const v3 P = ld3(x, pp), dP = ld3(p, pp);
-                    const C3 plo = cell_of(vmin(P, P + dP) - d, inv_dx);
-                    const C3 first = cmax(lo, plo);
-                    if (first.x != cx || first.y != cy || first.z != cz) continue;
                     if (!pt_aabb_moving(P, A, B, C, dP, dA, dB, dC, dh)) continue;
                     const double d2 = pt_dist2(P, A, B, C);
                     atomic_min_pos(alpha + (g.vscene ? sc : 0), pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, d2));
@@ -335,7 +412,7 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
 // compute_filter_3D_EE (NEWTON_IPC.py:409-440): edges query moving bbox +- dh
 __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
                                                 const double* __restrict__ p, double dh, SceneGeo g, double eta,
-                                                GridView gv, unsigned long long* __restrict__ alpha) {
+                                                GridView gv, CandView cv, unsigned long long* __restrict__ alpha) {
     // QG lanes per query edge share the candidates of each cell
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
     if (i >= nbe) return;
@@ -347,6 +424,7 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
     const v3 d = mk(dh, dh, dh);
     const v3 mn = vmin(vmin(A0, A0 + dA0), vmin(A1, A1 + dA1)), mx = vmax(vmax(A0, A0 + dA0), vmax(A1, A1 + dA1));
     const C3 lo = cell_of(mn - d, inv_dx), hi = cell_of(mx + d, inv_dx);
+    const float4 qlo = f32_lo(mn), qhi = f32_hi(mx);   // ee_aabb_moving's query edge box
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
             for (long long cz = lo.z; cz <= hi.z; ++cz) {
@@ -355,12 +433,13 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
                 for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
                     const int j = gv.ids[k];
                     if (!(i < j)) continue;
+                    const int4 sc4 = __ldg(cv.cell + j);
+                    const C3 first = cmax(lo, C3{sc4.x, sc4.y, sc4.z});
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (!f32_overlap(__ldg(cv.box + 2 * j), __ldg(cv.box + 2 * j + 1), qlo, qhi)) continue;
                     const int b0 = be[2 * j], b1 = be[2 * j + 1];
                     if (a0 == b0 || a0 == b1 || a1 == b0 || a1 == b1) continue;
                     const v3 B0 = ld3(x, b0), B1 = ld3(x, b1), dB0 = ld3(p, b0), dB1 = ld3(p, b1);
-                    const C3 slo = cell_of(vmin(vmin(B0, B0 + dB0), vmin(B1, B1 + dB1)), inv_dx);
-                    const C3 first = cmax(lo, slo);
-                    if (first.x != cx || first.y != cy || first.z != cz) continue;
                     if (!ee_aabb_moving(A0, A1, B0, B1, dA0, dA1, dB0, dB1, dh)) continue;
                     const double d2 = ee_dist2(A0, A1, B0, B1);
                     atomic_min_pos(alpha + (g.vscene ? sc : 0), ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2));
@@ -383,7 +462,7 @@ __global__ void __launch_bounds__(128) k_ccd_inversion(int nT, const int4* __res
 // check_collision_3d (NEWTON_IPC.py:855-880): triangles query bbox cells, edges hashed +- dh
 __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restrict__ bt, const int* __restrict__ be,
                                                    const double* __restrict__ x, double dh, SceneGeo g,
-                                                   GridView gv, int* __restrict__ hit) {
+                                                   GridView gv, CandView cv, int* __restrict__ hit) {
     // QG lanes per query triangle share the candidates of each cell
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
     if (i >= nbt) return;
@@ -392,8 +471,9 @@ __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restric
     const int sc = g.scene(t0);
     const double inv_dx = g.idx(sc);
     const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2);
-    const C3 lo = cell_of(vmin(vmin(A, B), C), inv_dx), hi = cell_of(vmax(vmax(A, B), C), inv_dx);
-    const v3 d = mk(dh, dh, dh);
+    const v3 tmn = vmin(vmin(A, B), C), tmx = vmax(vmax(A, B), C);
+    const C3 lo = cell_of(tmn, inv_dx), hi = cell_of(tmx, inv_dx);
+    const float4 qlo = f32_lo(tmn), qhi = f32_hi(tmx);   // the triangle's box; edges carry +- dh
     hit += g.vscene ? sc : 0;
     for (long long cx = lo.x; cx <= hi.x; ++cx)
         for (long long cy = lo.y; cy <= hi.y; ++cy)
@@ -403,12 +483,13 @@ __global__ void __launch_bounds__(128) k_collision(int nbt, const int* __restric
                 if (c < 0) continue;
                 for (int k = gv.us[c] + lane; k < gv.us[c + 1]; k += QG) {
                     const int j = gv.ids[k];
+                    const int4 sc4 = __ldg(cv.cell + j);
+                    const C3 first = cmax(lo, C3{sc4.x, sc4.y, sc4.z});
+                    if (first.x != cx || first.y != cy || first.z != cz) continue;
+                    if (!f32_overlap(__ldg(cv.box + 2 * j), __ldg(cv.box + 2 * j + 1), qlo, qhi)) continue;
                     const int a0 = be[2 * j], a1 = be[2 * j + 1];
                     if (a0 == t0 || a0 == t1 || a0 == t2 || a1 == t0 || a1 == t1 || a1 == t2) continue;
                     const v3 P = ld3(x, a0), Q = ld3(x, a1);
-                    const C3 slo = cell_of(vmin(P, Q) - d, inv_dx);
-                    const C3 first = cmax(lo, slo);
-                    if (first.x != cx || first.y != cy || first.z != cz) continue;
                     if (seg_tri(P, Q, A, B, C)) atomicOr(hit, 1);
                 }
             }
@@ -657,6 +738,9 @@ int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const dou
     int* ovf = g.ncells.as<int>() + 1;
     k_cell_count<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, sg, g.counts.as<long long>(), ovf);
     FIPC_LAUNCHED();
+    if (g.cell4.ensure(16ll * n) || g.box4.ensure(32ll * n)) return FIPC_ERR_CUDA;
+    k_cand_records<<<nblk(n, 256), 256, 0, s>>>(mode, n, prim, x, p, c->dhat, sg, g.cell4.as<int4>(), g.box4.as<float4>());
+    FIPC_LAUNCHED();
     long long* cnt = g.counts.as<long long>();
     long long* off = g.offsets.as<long long>();
     int st = cub_call(c, [&](void* t, size_t& b) { return cub::DeviceScan::ExclusiveSum(t, b, cnt, off, n, s); });
@@ -708,6 +792,8 @@ int build_grid(fipc_ctx* c, Grid& g, int mode, int n, const int* prim, const dou
     FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
 }
+
+static CandView cands(const Grid& g) { return CandView{g.cell4.as<int4>(), g.box4.as<float4>()}; }
 
 static GridView view(const Grid& g) {
     GridView v;
@@ -792,7 +878,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         if (st) return st;
         if (c->gp.n_entries > 0 && c->nBT > 0) {
             k_find_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, c->dhat, c->dhat2, sg,
-                                                         view(c->gp), sink);
+                                                         view(c->gp), cands(c->gp), sink);
             FIPC_LAUNCHED();
         }
         if (c->nBT > 0 && c->nBP > 0) {
@@ -803,7 +889,7 @@ int find_constraints(fipc_ctx* c, const double* x, cudaStream_t s) {
         if (st) return st;
         if (c->ge.n_entries > 0) {
             k_find_ee<<<nblk((long long)QG * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, c->x0, c->dhat, c->dhat2, sg,
-                                                         view(c->ge), sink);
+                                                         view(c->ge), cands(c->ge), sink);
             FIPC_LAUNCHED();
         }
         if (c->nBE > 1) {
@@ -836,7 +922,7 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     if (st) return st;
     if (c->gp.n_entries > 0 && c->nBT > 0) {
         k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, sg, eta,
-                                                    view(c->gp), slot);
+                                                    view(c->gp), cands(c->gp), slot);
         FIPC_LAUNCHED();
     }
     if (c->nBT > 0 && c->nBP > 0) {
@@ -846,7 +932,8 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     st = build_grid(c, c->ge, 3, c->nBE, c->be, x, p, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0) {
-        k_ccd_ee<<<nblk((long long)QG * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, view(c->ge), slot);
+        k_ccd_ee<<<nblk((long long)QG * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, view(c->ge), cands(c->ge),
+                                                                   slot);
         FIPC_LAUNCHED();
     }
     if (c->nBE > 1) {
@@ -884,7 +971,8 @@ int collision_launch(fipc_ctx* c, const double* x, int* hit, cudaStream_t s) {
     st = build_grid(c, c->ge, 4, c->nBE, c->be, x, nullptr, sg, s);
     if (st) return st;
     if (c->ge.n_entries > 0 && c->nBT > 0) {
-        k_collision<<<nblk((long long)QG * c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, sg, view(c->ge), hit);
+        k_collision<<<nblk((long long)QG * c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->be, x, c->dhat, sg, view(c->ge),
+                                                                       cands(c->ge), hit);
         FIPC_LAUNCHED();
     }
     if (c->nBT > 0 && c->nBE > 0) {
