@@ -58,7 +58,7 @@ def build(force=False, verbose=False, jobs=None):
     with cf.ThreadPoolExecutor(max_workers=jobs or min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
     tmp = LIB + f'.{os.getpid()}.tmp'
-    cmd = [cc, *ARCH, '-shared', '-o', tmp, *objs, '-lcudart', '-ldl']
+    cmd = [cc, *ARCH, '-shared', '-o', tmp, *objs, '-lcudart']
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f'link failed:\n{r.stdout}\n{r.stderr}')

@@ -73,3 +73,39 @@ def test_pcg_fallback_to_direct(newton_golden):
         finally:
             sim.close()
     assert out[0] == out[1]
+
+
+@pytest.mark.parametrize('case', ['lattice_216', 'bar_100'])
+def test_direct_matches_tight_pcg_on_large_scenes(case):
+    """Full-size lattice at its first ground contact and a 240k-tet bar a few steps into its
+    twist: hundreds to thousands of fronts over a dozen tree levels.  The direct direction
+    agrees with PCG at relative residual 1e-12 to 1e-8 of its largest entry."""
+    if case == 'lattice_216':
+        scene = scenes.predeform(scenes.cube_lattice(m=6, n=6, seed=0), 1e-4, 0)
+    else:
+        scene = scenes.twisted_bar(nx=100, ny=20, nz=20, size=(0.25, 0.05, 0.05), seed=1)
+    sim = NewtonIPC(scene, pcg_rtol=1e-8)
+    try:
+        f = 0
+        while f < 40:
+            sim.step(f)
+            f += 1
+            if case == 'bar_100' and f == 4:
+                break
+            if case == 'lattice_216' and sum(sim.counts) > 0:
+                break
+        sim.compute_xn_and_xTilde()
+        sim.move_nodes(f * sim.dt)
+        sim.find_constraints()
+        sim.compute_hessian_and_gradient()
+        sim.pcg_rtol, sim.pcg_maxit = 1e-12, 100000
+        sim.solve_system(f * sim.dt)
+        p_pcg = sim.data_sol.cpu().numpy().copy()
+        sim.solver = 'direct'
+        sim.solve_system(f * sim.dt)
+        p_dir = sim.data_sol.cpu().numpy().copy()
+        assert np.abs(p_dir - p_pcg).max() <= 1e-8 * np.abs(p_pcg).max()
+        fixed = sim.fixed.cpu().numpy().astype(bool)
+        assert np.all(p_dir.reshape(-1, 3)[fixed] == 0.0)
+    finally:
+        sim.close()
