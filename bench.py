@@ -47,10 +47,11 @@ def parse():
     ap.add_argument('--profile-kernel', type=int, default=1, help='kernel timed for the roofline (1 = PCG SpMV)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--cpu-sample-pcg', type=int, default=100000)
-    ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes', 'stack2d'],
+    ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes', 'stack2d', 'admm'],
                     help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context; '
                          'lattice: 216 cubes dropped on a ground box; cubes: two 8^3-hex cubes; '
-                         'stack2d: the 2D path, 16 squares of 16x16 quads on a ground segment')
+                         'stack2d: the 2D path, 16 squares of 16x16 quads on a ground segment; '
+                         'admm: the ADMM-IPC variant on the two-cube drop')
     ap.add_argument('--scenes', type=int, default=512, help='scenes of the batch workload')
     ap.add_argument('--learned-steps', type=int, default=20,
                     help='steps run from the timed state with the inertial and the learned start (0: skip)')
@@ -291,6 +292,8 @@ def main():
         return main_batch(args)
     if args.workload == 'stack2d':
         return main_2d(args)
+    if args.workload == 'admm':
+        return main_admm(args)
     if args.impl == 'reference':
         return run_reference(args)
     import numpy as np
@@ -705,6 +708,110 @@ def main_2d(args):
         v, sample = cpu_steps(snap[0].cpu().numpy(), snap[1].cpu().numpy(), f0)
         from oracle import oracle as O
         out['cpu_baseline'] = {'value': v, 'unit': 'steps/s', 'cores': O.lib().oracle_num_threads(), 'kind': 'port', 'sample': sample}
+    print(json.dumps(out), flush=True)
+    sim.close()
+
+
+ADMM_METRIC = 'steps/s (ADMM-IPC, two cubes, 6k tets)'
+
+
+def main_admm(args):
+    """ADMM-IPC (projects/FastIPC/ADMM_IPC.py, 20 ADMM iterations per step) on the two-cube drop
+    of 8^3 hexes per cube (configuration 0's geometry; fixed-corotated, as the script imports):
+    W warm-up steps, K timed steps (CUDA events), e2e with the state through pinned host memory;
+    the CPU oracle (numpy restatement) on the first ADMM iterations of the same step from the
+    same state, scaled to whole steps."""
+    from fastipc_gb300 import scenes as SC
+    rank = int(os.environ.get('RANK', '0'))
+    scene = SC.two_cubes(n=8, seed=0)
+    cfg = {'workload': 'ADMM-IPC: two 0.1 m cubes of 8x8x8 hexes x6 tets, upper one rotated (seed 0) and moving at -1 m/s; '
+                       'fixed-corotated E=1e5 nu=0.4, dhat=1e-3, dt=0.01, 20 ADMM iterations per step',
+           'tets': int(len(scene.tets)), 'verts': int(len(scene.x)), 'pcg_rtol': args.pcg_rtol,
+           'l2': 'working set smaller than L2, not flushed between steps (bound by launches and host syncs)'}
+
+    def cpu_sample(x0, v0, f0, iters=2):
+        from oracle.admm_oracle import AdmmOracle
+        o = AdmmOracle(scene)
+        o.x, o.v = x0.copy(), v0.copy()
+        t0 = time.perf_counter()
+        o.initial_guess()
+        for k in range(iters):
+            o.admm_iteration(f0, k)
+        dt = time.perf_counter() - t0
+        return iters / (dt * o.admm_iters), (f'ADMM iterations 0..{iters - 1} of step {f0} of the same scene from the same state '
+                                             f'({dt:.1f} s; numpy restatement, one core), scaled to 20 iterations per step')
+
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        from oracle.admm_oracle import AdmmOracle
+        o = AdmmOracle(scene)
+        for f in range(args.warmup):
+            o.step(f)
+        v, sample = cpu_sample(o.x, o.v, args.warmup)
+        print(json.dumps({'impl': 'reference', 'metric': ADMM_METRIC, 'value': v, 'unit': 'steps/s', 'n_gpus': args.gpus,
+                          'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True, 'scaling': 'weak',
+                          'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
+                          'cpu_baseline': {'value': v, 'unit': 'steps/s', 'cores': 1, 'kind': 'port', 'sample': sample},
+                          'e2e': {'value': v, 'unit': 'steps/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}), flush=True)
+        return
+    import torch
+    from fastipc_gb300 import _native
+    from fastipc_gb300.admm import AdmmIPC
+    from fastipc_gb300.build import build
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    build()
+    sim = AdmmIPC(scene, device=dev, pcg_rtol=args.pcg_rtol)
+    f = 0
+    for _ in range(args.warmup):
+        sim.step(f)
+        f += 1
+    snap = (sim.x.clone(), sim.v.clone())
+    f0 = f
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _native.launch_count()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.step(f)
+            f += 1
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = _native.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1)
+    hx = torch.empty_like(snap[0], device='cpu').pin_memory()
+    hv = torch.empty_like(snap[1], device='cpu').pin_memory()
+    hx.copy_(snap[0])
+    hv.copy_(snap[1])
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    f = f0
+    for _ in range(args.steps):
+        sim.x.copy_(hx, non_blocking=True)
+        sim.v.copy_(hv, non_blocking=True)
+        sim.step(f)
+        hx.copy_(sim.x, non_blocking=True)
+        hv.copy_(sim.v, non_blocking=True)
+        f += 1
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1)
+    nbytes = 2 * sim.x.numel() * 8
+    its = sim.global_iters[-args.steps * sim.admm_iters:]
+    out = {'metric': ADMM_METRIC, 'value': args.steps / (ms / 1e3), 'unit': 'steps/s', 'n_gpus': 1, 'steps': args.steps,
+           'warmup': args.warmup, 'ms_per_step': ms / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+           'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
+           'ms_per_admm_iter': ms / (args.steps * sim.admm_iters), 'pcg_iters_per_global_step': sum(its) / max(len(its), 1),
+           'e2e': {'value': args.steps / (e2e_ms / 1e3), 'unit': 'steps/s', 'h2d_bytes_per_step': nbytes, 'd2h_bytes_per_step': nbytes},
+           'gpu_launches': launches, 'clocks': clk.summary()}
+    if not args.no_cpu_baseline:
+        v, sample = cpu_sample(snap[0].cpu().numpy(), snap[1].cpu().numpy(), f0)
+        out['cpu_baseline'] = {'value': v, 'unit': 'steps/s', 'cores': 1, 'kind': 'port', 'sample': sample}
     print(json.dumps(out), flush=True)
     sim.close()
 

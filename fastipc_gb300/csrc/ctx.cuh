@@ -153,6 +153,13 @@ __device__ __forceinline__ v3 ld3(const double* __restrict__ x, int i) {
 }
 #endif
 
+// row ranges of the concatenated lists: rows [row0[t], row0[t+1]) are of type t and their
+// nv(t)^2 blocks start at ent0[t] + (r - row0[t]) nv(t)^2
+struct TypeTable {
+    int row0[N_TYPES + 1];
+    long long ent0[N_TYPES + 1];
+};
+
 constexpr int RED_BLOCKS = 304;     // 2 x 152 SMs: fixed reduction grid (deterministic sums)
 constexpr int RED_THREADS = 256;
 

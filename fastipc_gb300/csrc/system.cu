@@ -101,13 +101,6 @@ __global__ void k_assemble_rhs(int nV, const int* __restrict__ vt_ptr, const int
 }
 
 // ---------------------------------------------------------------- contact blocks
-// row ranges of the concatenated lists: rows [row0[t], row0[t+1]) are of type t and their
-// nv(t)^2 blocks start at ent0[t] + (r - row0[t]) nv(t)^2
-struct TypeTable {
-    int row0[N_TYPES + 1];
-    long long ent0[N_TYPES + 1];
-};
-
 // one thread per constraint row (global index over the concatenated lists)
 __global__ void k_contact_keys(int n_rows, const int4* __restrict__ rows, TypeTable tt, unsigned long long* __restrict__ keys,
                                int* __restrict__ vals) {
@@ -381,24 +374,59 @@ int cs_offsets(fipc_ctx* c, const double* x, cudaStream_t s);
 int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t s);
 void cs_apply(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s);
 
+int contact_prepare(fipc_ctx* c, TypeTable* tt, int* nrows_out, long long* nent_out, cudaStream_t s);
+
+// the elastic + inertia matrix (sliced ELL) from the element blocks in elem_H (tiled layout)
+// and the lumped mass on the diagonal blocks
+int assemble_elastic(fipc_ctx* c, cudaStream_t s) {
+    k_assemble_elastic<<<nblk(c->n_upper, 128), 128, 0, s>>>(c->n_upper, c->up_cptr, c->up_contrib, c->up_spos, c->up_tspos,
+                                                             c->up_row, c->elem_H, c->mass, c->sell_val);
+    FIPC_LAUNCHED();
+    FIPC_CUDA(cudaGetLastError());
+    return FIPC_OK;
+}
+int contact_reduce(fipc_ctx* c, const TypeTable& tt, int nrows, long long nent, cudaStream_t s);
+
 // compute_hessian_and_gradient (NEWTON_IPC.py:736-747) for the current constraint lists
 int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t s) {
     int st = cs_offsets(c, x, s);
     if (st) return st;
     st = launch_elasticity(c->nT, c->tets, x, c->dminv, c->vol, c->lam, c->mu, c->dt, nullptr, c->elem_g, c->elem_H, s, true);
     if (st) return st;
-    k_assemble_elastic<<<nblk(c->n_upper, 128), 128, 0, s>>>(c->n_upper, c->up_cptr, c->up_contrib, c->up_spos, c->up_tspos,
-                                                             c->up_row, c->elem_H, c->mass, c->sell_val);
-    FIPC_LAUNCHED();
+    st = assemble_elastic(c, s);
+    if (st) return st;
     k_assemble_rhs<<<nblk(c->nV, 128), 128, 0, s>>>(c->nV, c->vt_ptr, c->vt_list, c->elem_g, c->mass, x, xt, c->rhs);
     FIPC_LAUNCHED();
-    // contact rows, concatenated in list order
+    TypeTable tt;
+    int nrows = 0;
+    long long nent = 0;
+    st = contact_prepare(c, &tt, &nrows, &nent, s);
+    if (st || nrows == 0) return st;
+    // the rows' barrier gradients / projected Hessians
+    for (int t = 0; t < N_TYPES; ++t) {
+        if (!c->h_counts[t]) continue;
+        const int off = tt.row0[t];
+        st = launch_barrier_rows(t, c->h_counts[t], c->rows[t].as<int>(), x, c->x0, c->dhat2, c->kappa,
+                                 c->n_scenes > 1 ? c->s_kappa : nullptr, c->v_scene, nullptr,
+                                 c->c_g.as<double>() + 12ll * off, c->c_H.as<double>() + 144ll * off, nullptr, s);
+        if (st) return st;
+    }
+    return contact_reduce(c, tt, nrows, nent, s);
+}
+
+// The contact rows of the current lists, concatenated in list order into rows_tmp: the type
+// table, the row and block-entry counts, and buffers for the per-row gradients c_g [rows][12]
+// and 3x3 blocks c_H [rows][16][9] that the caller fills.  With no rows the contact matrix is
+// left empty.
+int contact_prepare(fipc_ctx* c, TypeTable* tt, int* nrows_out, long long* nent_out, cudaStream_t s) {
     int nrows = 0;
     long long nent = 0;
     for (int t = 0; t < N_TYPES; ++t) {
         nrows += c->h_counts[t];
         nent += (long long)c->h_counts[t] * type_nverts(t) * type_nverts(t);
     }
+    *nrows_out = nrows;
+    *nent_out = nent;
     c->c_rows = nrows;
     c->c_nnzb = 0;
     if (c->c_rowptr.ensure(4ll * (c->nV + 1))) return FIPC_ERR_CUDA;
@@ -411,32 +439,31 @@ int assemble_system(fipc_ctx* c, const double* x, const double* xt, cudaStream_t
         c->c_vals.ensure(4 * nent) || c->c_vals_alt.ensure(4 * nent) || c->c_ukeys.ensure(8 * nent) || c->c_ucount.ensure(4 * (nent + 1)) ||
         c->c_ustart.ensure(4 * (nent + 1)) || c->c_val.ensure(72 * nent) || c->c_col.ensure(4 * nent) || c->rows_tmp.ensure(16ll * nrows))
         return FIPC_ERR_CUDA;
-    // concatenated rows (list order) and their barrier gradients / projected Hessians
     int4* all = c->rows_tmp.as<int4>();
-    TypeTable tt;
     int off = 0;
     long long eoff = 0;
     for (int t = 0; t < N_TYPES; ++t) {
-        tt.row0[t] = off;
-        tt.ent0[t] = eoff;
-        if (c->h_counts[t]) {
-            FIPC_CUDA(cudaMemcpyAsync(all + off, c->rows[t].p, 16ll * c->h_counts[t], cudaMemcpyDeviceToDevice, s));
-            st = launch_barrier_rows(t, c->h_counts[t], c->rows[t].as<int>(), x, c->x0, c->dhat2, c->kappa,
-                                     c->n_scenes > 1 ? c->s_kappa : nullptr, c->v_scene, nullptr,
-                                     c->c_g.as<double>() + 12ll * off, c->c_H.as<double>() + 144ll * off, nullptr, s);
-            if (st) return st;
-        }
+        tt->row0[t] = off;
+        tt->ent0[t] = eoff;
+        if (c->h_counts[t]) FIPC_CUDA(cudaMemcpyAsync(all + off, c->rows[t].p, 16ll * c->h_counts[t], cudaMemcpyDeviceToDevice, s));
         off += c->h_counts[t];
         eoff += (long long)c->h_counts[t] * type_nverts(t) * type_nverts(t);
     }
-    tt.row0[N_TYPES] = off;
-    tt.ent0[N_TYPES] = eoff;
+    tt->row0[N_TYPES] = off;
+    tt->ent0[N_TYPES] = eoff;
+    return FIPC_OK;
+}
+
+// The contact matrix (block CSR, fixed-order sums of every (row, column) block of the rows) and
+// the rows' gradients folded into rhs, from c_g / c_H filled for the rows contact_prepare set up
+int contact_reduce(fipc_ctx* c, const TypeTable& tt, int nrows, long long nent, cudaStream_t s) {
+    const int4* all = c->rows_tmp.as<int4>();
     k_contact_keys<<<nblk(nrows, 128), 128, 0, s>>>(nrows, all, tt, c->c_keys.as<unsigned long long>(), c->c_vals.as<int>());
     FIPC_LAUNCHED();
     const int N = (int)nent;
     cub::DoubleBuffer<unsigned long long> kb(c->c_keys.as<unsigned long long>(), c->c_keys_alt.as<unsigned long long>());
     cub::DoubleBuffer<int> vb(c->c_vals.as<int>(), c->c_vals_alt.as<int>());
-    st = cub_call(c, [&](void* tm, size_t& b) { return cub::DeviceRadixSort::SortPairs(tm, b, kb, vb, N, 0, 53, s); });
+    int st = cub_call(c, [&](void* tm, size_t& b) { return cub::DeviceRadixSort::SortPairs(tm, b, kb, vb, N, 0, 53, s); });
     if (st) return st;
     unsigned long long* sk = kb.Current();
     int* sv = vb.Current();

@@ -112,9 +112,10 @@ int fipc_solve_system(fipc_ctx* ctx, const unsigned char* fixed, double rtol, in
 /* output_residual, NEWTON_IPC.py:805-812: max |sol| */
 /* solve_system by a sparse Cholesky factorisation instead of PCG: the reference's CHOLMOD solve
  * (NEWTON_IPC.py:758-776) for the assembled system with its Dirichlet edit, for iterations
- * where fipc_solve_system reaches its iteration limit.  The factorisation is cuSOLVER's, opened
- * at run time: status 4 when it is not available, 3 when the system is not positive definite.
- * nnz_h (may be NULL): scalar non-zeros factorised. */
+ * where fipc_solve_system reaches its iteration limit.  A multifrontal factorisation on the GPU
+ * (nested-dissection ordering on the host); status 3 when the system is not positive definite,
+ * 1 when its fronts do not fit in free device memory.  nnz_h (may be NULL): entries stored in
+ * the factor's fronts (lower triangles), saturated at INT_MAX. */
 int fipc_solve_system_direct(fipc_ctx* ctx, const unsigned char* fixed, double* sol, int* nnz_h, void* stream);
 int fipc_output_residual(fipc_ctx* ctx, const double* sol, double* res_h, void* stream);
 
@@ -149,6 +150,39 @@ int fipc_compute_intersection_free_step_size(fipc_ctx* ctx, const double* x, con
 
 /* check_collision, NEWTON_IPC.py:855-886 */
 int fipc_check_collision(fipc_ctx* ctx, const double* x, int* hit_h, void* stream);
+
+/* ---- ADMM-IPC (projects/FastIPC/ADMM_IPC.py) ----------------------------------------------
+ * The ADMM variant of the time step on a context (fixed-corotated elasticity, as the script
+ * imports).  Per tet: W [T], z [T][9], u [T][9].  Per constraint row of the current lists, in
+ * list order (the seven lists concatenated): y, r [n][9] (the row's nv-1 relative vectors
+ * x_c0 - x_ck, padded to 3) and Q [n].  The caller runs the iteration loop (ADMM_IPC.py:
+ * 1471-1526): fipc_find_constraints, fipc_admm_reuse, fipc_admm_global, the CCD filter
+ * (fipc_compute_intersection_free_step_size without the inversion filter, and
+ * fipc_check_collision), fipc_admm_local, fipc_admm_dual. */
+/* initial_guess, ADMM_IPC.py:296-313: W, z = F(xtilde), u = 0 */
+int fipc_admm_init(fipc_ctx* ctx, const double* xtilde, double* W, double* z, double* u, void* stream);
+/* reuse_admm_variables, ADMM_IPC.py:1230-1388, for the lists of the last find_constraints:
+ * old_counts_h [7] and old_rows [n_old][4] (the previous lists, concatenated in list order)
+ * with their old_y, old_r, old_Q; fills y, r, Q of the current rows. */
+int fipc_admm_reuse(fipc_ctx* ctx, double alpha, const double* x, const double* xtilde, const int* old_counts_h,
+                    const int* old_rows, const double* old_y, const double* old_r, const double* old_Q, double* y, double* r,
+                    double* Q, void* stream);
+/* global_step + global_PP..PEM + solve_system, ADMM_IPC.py:388-631: assembles the SPD system
+ * (mass, W^2 G G^T per tet, Q^2 E^T E per row) and solves it by PCG to relative residual rtol;
+ * x holds the guess on entry with the Dirichlet targets at the fixed vertices, which keep them,
+ * and the solution on return. */
+int fipc_admm_global(fipc_ctx* ctx, const double* xtilde, const double* W, const double* z, const double* u, const double* y,
+                     const double* r, const double* Q, const unsigned char* fixed, double rtol, int maxit, double* x,
+                     int* iters_h, void* stream);
+/* local_elasticity + local_PP..PEM, ADMM_IPC.py:633-960: updates z and y.  The reference's
+ * local loops are unbounded; here each stops after 256 Newton iterations or 64 halvings (a row
+ * with an indefinite Hessian can take steps that never fall below the tolerance).  detail_h
+ * (may be null) receives the bits: 1 / 2 a tet reached its Newton / halving bound, 4 / 8 a row,
+ * 16 a non-finite z or y.  Status 3 when a result is not finite. */
+int fipc_admm_local(fipc_ctx* ctx, const double* x, const double* W, double* z, const double* u, double* y, const double* r,
+                    const double* Q, int* detail_h, void* stream);
+/* dual_step, ADMM_IPC.py:962-994: u += F(x) - z, r += (x_c0 - x_ck) - y */
+int fipc_admm_dual(fipc_ctx* ctx, const double* x, const double* z, double* u, const double* y, double* r, void* stream);
 
 /* ---- learned Newton warm start (no counterpart in the reference) ----------------------------
  * A per-vertex MLP 55 (padded 64) -> 128 -> 128 -> 128 -> 3 (padded 4), GELU, FP32, parameters
