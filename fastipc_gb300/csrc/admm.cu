@@ -208,6 +208,12 @@ __global__ void k_admm_local_elastic(int nT, const int4* __restrict__ tets, cons
             for (int i = 0; i < 3; ++i) sg[i] = q0[i] + alpha * p[i];
             E = energy(sg);
         }
+        // a step that left sigma exactly where it was repeats itself in every later iteration:
+        // the loop would run to its bound without moving, so stop here with the same result
+        if (!converged && sg[0] == q0[0] && sg[1] == q0[1] && sg[2] == q0[2]) {
+            atomicOr(status, ADMM_ELASTIC_NEWTON);
+            break;
+        }
     }
     bool finite = true;
     for (int i = 0; i < 3; ++i)
@@ -354,17 +360,22 @@ __global__ void k_admm_global_rows(int n, TypeTable tt, const double* __restrict
 
 // local_PP .. local_PEM (ADMM_IPC.py:668-960): per row, Newton in the relative vectors pos on
 // barrier(pos) + Q^2 / 2 |pos - (x-relative + r)|^2, regularised solve_N steps, halving while
-// the energy rises; y = pos
-__global__ void k_admm_local_rows(int n, const int4* __restrict__ rows, TypeTable tt, const double* __restrict__ x,
-                                  const double* __restrict__ x0, double dh2, double kappa, const double* __restrict__ Q,
-                                  const double* __restrict__ r, double* __restrict__ y, int* __restrict__ status) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+// the energy rises; y = pos.  One warp per row: lane 0 forms the Newton step, then the lanes
+// evaluate the energy at the step sizes 2^-k for k = lane, 32 + lane and 64 at once, and the
+// smallest k whose energy does not rise is taken -- the step size, and every bit of the new
+// point, the sequential halving loop would reach.
+__global__ void __launch_bounds__(64) k_admm_local_rows(int n, const int4* __restrict__ rows, TypeTable tt, const double* __restrict__ x,
+                                                        const double* __restrict__ x0, double dh2, double kappa, const double* __restrict__ Q,
+                                                        const double* __restrict__ r, double* __restrict__ y, int* __restrict__ status) {
+    const int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (c >= n) return;
+    const unsigned full = 0xffffffffu;
     const int t = row_type(tt, c);
     const int nv = type_nverts(t), m = 3 * (nv - 1);
     const int4 q = rows[c];
     const int id[4] = {q.x, q.y, q.z, q.w};
     double pos[9], tgt[9];
+    for (int k = 0; k < 9; ++k) pos[k] = tgt[k] = 0.0;
     for (int k = 1; k < nv; ++k) {
         const v3 d = ld3(x, id[0]) - ld3(x, id[k]);
         const double dd[3] = {d.x, d.y, d.z};
@@ -383,49 +394,75 @@ __global__ void k_admm_local_rows(int n, const int4* __restrict__ rows, TypeTabl
         for (int i = 0; i < m; ++i) s += (ps[i] - tgt[i]) * (ps[i] - tgt[i]);
         return E + s * q2 / 2;
     };
+    int stat = 0;
     bool converged = false;
     int it = 0;
     while (!converged) {
         if (++it > ADMM_MAX_NEWTON) {
-            atomicOr(status, ADMM_ROW_NEWTON);
+            stat |= ADMM_ROW_NEWTON;
             break;
         }
-        double E, g[9], P[81];
-        rel_row(t, pos, X0, dh2, kappa, &E, g, P, nullptr);
-        for (int i = 0; i < m; ++i) {
-            g[i] += (pos[i] - tgt[i]) * q2;
-            P[i * m + i] += q2;
-        }
-        double p[9];
-        solve_n(m, P, g, p);
-        double pp = 0.0;
-        for (int i = 0; i < m; ++i) {
-            p[i] = -p[i];
-            pp += p[i] * p[i];
-        }
-        if (pp < 1e-6) converged = true;
-        double alpha = 1.0, p0[9];
-        for (int i = 0; i < m; ++i) p0[i] = pos[i];
-        const double E0 = energy(p0);
-        for (int i = 0; i < m; ++i) pos[i] = p0[i] + p[i];
-        double E1 = energy(pos);
-        int k = 0;
-        while (E1 > E0) {
-            if (++k > ADMM_MAX_HALVINGS) {
-                atomicOr(status, ADMM_ROW_HALVING);
-                break;
+        double p[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0}, E0 = 0.0;
+        int conv = 0;
+        if (lane == 0) {
+            double E, g[9], P[81];
+            rel_row(t, pos, X0, dh2, kappa, &E, g, P, nullptr);
+            for (int i = 0; i < m; ++i) {
+                g[i] += (pos[i] - tgt[i]) * q2;
+                P[i * m + i] += q2;
             }
-            alpha *= 0.5;
-            for (int i = 0; i < m; ++i) pos[i] = p0[i] + alpha * p[i];
-            E1 = energy(pos);
+            solve_n(m, P, g, p);
+            double pp = 0.0;
+            for (int i = 0; i < m; ++i) {
+                p[i] = -p[i];
+                pp += p[i] * p[i];
+            }
+            conv = pp < 1e-6;
+            E0 = energy(pos);
+        }
+        for (int i = 0; i < 9; ++i) p[i] = __shfl_sync(full, p[i], 0);
+        E0 = __shfl_sync(full, E0, 0);
+        converged = __shfl_sync(full, conv, 0) != 0;
+        double p0[9];
+        for (int i = 0; i < 9; ++i) p0[i] = pos[i];
+        // step sizes 2^-k, k = 0 .. ADMM_MAX_HALVINGS: the first whose energy does not rise
+        int kstar = -1;
+        for (int base = 0; base <= ADMM_MAX_HALVINGS && kstar < 0; base += 32) {
+            const int k = base + lane;
+            bool ok = false;
+            if (k <= ADMM_MAX_HALVINGS) {
+                double alpha = 1.0, ps[9];
+                for (int h = 0; h < k; ++h) alpha *= 0.5;
+                for (int i = 0; i < m; ++i) ps[i] = k == 0 ? p0[i] + p[i] : p0[i] + alpha * p[i];
+                ok = !(energy(ps) > E0);
+            }
+            const unsigned bal = __ballot_sync(full, ok);
+            if (bal) kstar = base + __ffs(bal) - 1;
+        }
+        if (kstar < 0) {
+            kstar = ADMM_MAX_HALVINGS;
+            stat |= ADMM_ROW_HALVING;
+        }
+        double alpha = 1.0;
+        for (int h = 0; h < kstar; ++h) alpha *= 0.5;
+        for (int i = 0; i < m; ++i) pos[i] = kstar == 0 ? p0[i] + p[i] : p0[i] + alpha * p[i];
+        // a step that left pos exactly where it was repeats itself in every later iteration:
+        // the loop would run to its bound without moving, so stop here with the same result
+        bool same = true;
+        for (int i = 0; i < m; ++i) same = same && pos[i] == p0[i];
+        if (!converged && same) {
+            stat |= ADMM_ROW_NEWTON;
+            break;
         }
     }
+    if (lane != 0) return;
     bool finite = true;
     for (int i = 0; i < m; ++i) {
         finite = finite && isfinite(pos[i]);
         y[9 * (size_t)c + i] = pos[i];
     }
-    if (!finite) atomicOr(status, ADMM_NONFINITE);
+    if (!finite) stat |= ADMM_NONFINITE;
+    if (stat) atomicOr(status, stat);
 }
 
 // dual_step, constraint part (ADMM_IPC.py:968-994): r_k += (x_c0 - x_ck) - y_k
@@ -564,7 +601,7 @@ int fipc_admm_local(fipc_ctx* c, const double* x, const double* W, double* z, co
     if (st) return st;
     if (n > 0) {
         if (!y || !r || !Q) return FIPC_ERR_ARGUMENT;
-        k_admm_local_rows<<<nblk_a(n, 64), 64, 0, s>>>(n, c->rows_tmp.as<int4>(), tt, x, c->x0, c->dhat2, c->kappa, Q, r, y, status);
+        k_admm_local_rows<<<nblk_a(32ll * n, 64), 64, 0, s>>>(n, c->rows_tmp.as<int4>(), tt, x, c->x0, c->dhat2, c->kappa, Q, r, y, status);
         FIPC_LAUNCHED();
     }
     int h = 0;

@@ -339,6 +339,8 @@ class AdmmOracle(O.OracleSim):
                     E = energy(s)
                 if done:
                     break
+                if np.array_equal(s, s_0):
+                    break           # no movement: every later iteration repeats this one
             self.z[e] = (U @ np.diag(s) @ V.T).ravel()
 
     def local_rows(self):
@@ -375,6 +377,8 @@ class AdmmOracle(O.OracleSim):
                         E = energy(pos)
                     if done:
                         break
+                    if np.array_equal(pos, p0):
+                        break       # no movement: every later iteration repeats this one
                 self.y[c, :m] = pos
                 c += 1
 
