@@ -46,12 +46,15 @@ def parse():
     ap.add_argument('--warm-start', type=int, default=1, help='PCG initial guess from the previous step (1) or zero (0)')
     ap.add_argument('--profile-kernel', type=int, default=1, help='kernel timed for the roofline (1 = PCG SpMV)')
     ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--precond', default='multigrid', choices=['multigrid', 'two-level'],
+                    help='PCG preconditioner of the bar, lattice and cube workloads')
     ap.add_argument('--cpu-sample-pcg', type=int, default=100000)
-    ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes', 'stack2d', 'admm'],
+    ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes', 'stack2d', 'admm', 'direct'],
                     help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context; '
                          'lattice: 216 cubes dropped on a ground box; cubes: two 8^3-hex cubes; '
                          'stack2d: the 2D path, 16 squares of 16x16 quads on a ground segment; '
-                         'admm: the ADMM-IPC variant on the two-cube drop')
+                         'admm: the ADMM-IPC variant on the two-cube drop; '
+                         'direct: the direct (multifrontal Cholesky) solve of the lattice\'s Newton system at first contact')
     ap.add_argument('--scenes', type=int, default=512, help='scenes of the batch workload')
     ap.add_argument('--learned-steps', type=int, default=20,
                     help='steps run from the timed state with the inertial and the learned start (0: skip)')
@@ -195,10 +198,14 @@ def restore(sim, snap):
     sim._dir_hist = {k: v.clone() for k, v in snap[3].items()}
 
 
-def cpu_baseline(scene, newton_per_step, pcg_per_newton, args):
+def cpu_baseline(scene, newton_per_step, pcg_per_newton, args, spmv_per_iter=1):
     """The oracle on the host cores: one Newton iteration of time step 1 of the same scene
-    (constraints, assembly, full PCG solve, line search), scaled to steps/s with the Newton and
-    PCG iteration counts of the timed GPU steps (the same algorithm)."""
+    (constraints, assembly, full PCG solve, line search), scaled to steps/s with the Newton
+    iteration count of the timed GPU steps.  `value`: the CPU credited with the GPU's PCG
+    iteration count times the fine-level products each GPU iteration makes (spmv_per_iter: 1 for
+    block-Jacobi or the two-level preconditioner, 3 for a multigrid V(1,1)-cycle), at the cost of
+    its own block-Jacobi iterations; `own_solver_value`: its own block-Jacobi PCG to the same
+    tolerance."""
     from oracle import oracle as O
     sim = O.OracleSim(scene, solver='bsr', pcg_rtol=args.pcg_rtol, pcg_maxit=args.cpu_sample_pcg)
     sim.step(0, max_newton=1)                 # rest state (zero right-hand side)
@@ -222,17 +229,19 @@ def cpu_baseline(scene, newton_per_step, pcg_per_newton, args):
     pcg_its = max(sim.pcg_iters[-1], 1)
     t_fixed = (t1 - t0) + (t3 - t2)
     t_pcg_it = (t2 - t1) / pcg_its
-    t_newton = t_fixed + t_pcg_it * pcg_per_newton
+    t_newton = t_fixed + t_pcg_it * pcg_per_newton * spmv_per_iter
     sps = 1.0 / (t_newton * newton_per_step)
     t_own = t_fixed + t_pcg_it * pcg_its
     _ = E0
     return {'value': sps, 'unit': 'steps/s', 'cores': O.lib().oracle_num_threads(), 'kind': 'port',
             'sample': (f'one Newton iteration of step 1 of the same scene on the host cores ({t3 - t0:.1f} s: '
                        f'assembly+constraints+line search {t_fixed:.2f} s, PCG {pcg_its} its at {1e3 * t_pcg_it:.2f} ms/it); '
-                       f'scaled by the timed GPU steps\' {newton_per_step:.2f} Newton its/step and {pcg_per_newton:.0f} PCG its/Newton'),
+                       f'scaled by the timed GPU steps\' {newton_per_step:.2f} Newton its/step and {pcg_per_newton:.0f} PCG its/Newton '
+                       f'x {spmv_per_iter} fine-level products each'),
             'ms_per_newton_iter': 1e3 * t_newton,
-            'matched_iterations': ('value: the CPU is credited with the GPU preconditioner\'s PCG iteration count '
-                                   '(the same algorithm on both sides)'),
+            'matched_iterations': ('value: the CPU is credited with the GPU\'s PCG iteration count times the fine-level '
+                                   'matrix products of each GPU iteration, at the cost of one of its own block-Jacobi '
+                                   'iterations per product'),
             'own_solver_value': 1.0 / (t_own * newton_per_step),
             'own_solver': (f'the oracle\'s own block-Jacobi PCG ({pcg_its} its per Newton iteration in the sample), the '
                            f'solver the reference arm (--impl reference) runs'),
@@ -292,6 +301,8 @@ def main():
         return main_batch(args)
     if args.workload == 'stack2d':
         return main_2d(args)
+    if args.workload == 'direct':
+        return main_direct(args)
     if args.workload == 'admm':
         return main_admm(args)
     if args.impl == 'reference':
@@ -314,6 +325,9 @@ def main():
     build()
     scene = make_scene(args)
     sim = NewtonIPC(scene, device=dev, pcg_rtol=args.pcg_rtol, pcg_warm_start=bool(args.warm_start))
+    if args.precond == 'two-level':
+        sim.set_preconditioner(2048)
+    mg = sim.multigrid()
 
     def barrier():
         if dist is not None:
@@ -412,9 +426,12 @@ def main():
                 'time_share_of_step': pt / prof_ms if prof_ms > 0 else None}
         if note:
             roof['traffic_note'] = note
+        cfg = workload(args)
+        cfg['preconditioner'] = (f'multigrid V(1,1), {mg["levels"]} levels of {mg["nodes"]} nodes' if mg['levels']
+                                 else 'two-level additive (rigid-body modes of 2048-vertex runs)')
         out = {'metric': metric(args), 'value': value, 'unit': 'steps/s', 'n_gpus': world, 'steps': args.steps,
                'warmup': args.warmup, 'ms_per_step': ms_max / args.steps, 'higher_is_better': True, 'scaling': 'weak',
-               'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': workload(args),
+               'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
                'ms_per_newton_iter': ms_max / max(sum(newton), 1), 'newton_iters_per_step': newton_per_step,
                'pcg_iters_per_newton': pcg_per_newton, 'parallelism': 'replicas' if world > 1 else 'single',
                'e2e': {'value': world * args.steps / (e2e_ms / 1e3), 'unit': 'steps/s', 'h2d_bytes_per_step': nbytes,
@@ -426,7 +443,7 @@ def main():
         if learned:
             out['learned_warm_start'] = learned
         if world == 1 and not args.no_cpu_baseline:
-            out['cpu_baseline'] = cpu_baseline(scene, newton_per_step, pcg_per_newton, args)
+            out['cpu_baseline'] = cpu_baseline(scene, newton_per_step, pcg_per_newton, args, 3 if mg['levels'] else 1)
             if traj and traj.get('gpu_states') is not None:
                 traj.update(trajectory_cpu(scene, traj.pop('gpu_states'), args))
         if traj:
@@ -814,6 +831,142 @@ def main_admm(args):
         out['cpu_baseline'] = {'value': v, 'unit': 'steps/s', 'cores': 1, 'kind': 'port', 'sample': sample}
     print(json.dumps(out), flush=True)
     sim.close()
+
+
+DIRECT_METRIC = 'direct solves/s (216-cube lattice Newton system at first ground contact)'
+
+
+def main_direct(args):
+    """The direct solve of the Newton system (the reference's CHOLMOD role, NEWTON_IPC.py:764-776):
+    the 216-cube lattice (configuration 1's scene) stepped with PCG until its first ground
+    contact, then its assembled system (elastic and contact blocks) factorised and solved K times
+    after W warm-up solves.  A step is one whole direct solve: host analysis, factorisation and
+    substitution.  e2e: positions from pinned host memory, assembly, direct solve, direction back.
+    The roofline is the factorisation's FP64 flops over the solve time against the measured FP64
+    peak.  The CPU arm is the oracle's direct solve (scipy SuperLU) of the same system."""
+    from fastipc_gb300 import scenes as SC
+    rank = int(os.environ.get('RANK', '0'))
+    scene = SC.cube_lattice(m=6, n=6, seed=0)
+    cfg = {'workload': 'direct solve of the Newton system of the 6x6x6 lattice of 0.1 m cubes (6 hexes per side x6 tets) on its '
+                       'ground box at its first ground contact (PCG steps before it); NH E=1e5 nu=0.4, dhat=1e-3, dt=0.01',
+           'tets': int(len(scene.tets)), 'verts': int(len(scene.x)),
+           'l2': 'inputs larger than L2 (the fronts hold several GB)'}
+
+    def cpu_solve(x, v, f):
+        from oracle import oracle as O
+        o = O.OracleSim(scene, solver='direct')
+        o.x, o.v = x.copy(), v.copy()
+        o.compute_xn_and_xTilde()
+        o.move_nodes(f * o.dt)
+        o.find_constraints()
+        o.compute_hessian_and_gradient()
+        t0 = time.perf_counter()
+        o.solve_system(f * o.dt)
+        dt = time.perf_counter() - t0
+        return 1.0 / dt, f'one direct solve of the same system by the oracle (scipy SuperLU, {dt:.1f} s, one core)'
+
+    import numpy as np
+    if args.impl == 'reference':
+        if rank != 0:
+            return
+        from oracle import oracle as O
+        o = O.OracleSim(scene, solver='bsr', pcg_rtol=1e-8, pcg_maxit=400000)
+        f = 0
+        while f < 40:
+            o.step(f)
+            f += 1
+            if sum(len(r) for r in o.rows) > 0:
+                break
+        v, sample = cpu_solve(o.x, o.v, f)
+        print(json.dumps({'impl': 'reference', 'metric': DIRECT_METRIC, 'value': v, 'unit': 'solves/s', 'n_gpus': args.gpus,
+                          'steps': args.steps, 'warmup': args.warmup, 'higher_is_better': True, 'scaling': 'weak',
+                          'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'config': cfg,
+                          'cpu_baseline': {'value': v, 'unit': 'solves/s', 'cores': 1, 'kind': 'port', 'sample': sample},
+                          'e2e': {'value': v, 'unit': 'solves/s', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}), flush=True)
+        return
+    import torch
+    from fastipc_gb300 import _native
+    from fastipc_gb300.build import build
+    from fastipc_gb300.newton import NewtonIPC
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    build()
+    sim = NewtonIPC(scene, device=dev, pcg_rtol=1e-8)
+    f = 0
+    while f < 40:
+        sim.step(f)
+        f += 1
+        if sum(sim.counts) > 0:
+            break
+    x_h, v_h = sim.x.cpu().numpy().copy(), sim.v.cpu().numpy().copy()
+    t = f * sim.dt
+    sim.compute_xn_and_xTilde()
+    sim.move_nodes(t)
+    sim.find_constraints()
+    sim.compute_hessian_and_gradient()
+    sim.solver = 'direct'
+    for _ in range(args.warmup):
+        sim.solve_system(t)
+    stream = torch.cuda.current_stream(dev)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = _native.launch_count()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            sim.solve_system(t)
+        ev1.record(stream)
+        torch.cuda.synchronize(dev)
+    launches = _native.launch_count() - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    st = sim.direct_stats()
+    p_dir = sim.data_sol.clone()
+    sim.solver = 'pcg'
+    sim.pcg_rtol, sim.pcg_maxit = 1e-12, 200000
+    sim.solve_system(t)
+    agree = float(((p_dir - sim.data_sol).abs().max() / sim.data_sol.abs().max()).item())
+    sim.solver = 'direct'
+    # e2e: state from pinned host memory, assembly, direct solve, direction back to the host
+    xs = sim.x.clone()
+    hx = torch.empty_like(xs, device='cpu').pin_memory()
+    hx.copy_(xs)
+    hp = torch.empty_like(sim.data_sol, device='cpu').pin_memory()
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        sim.x.copy_(hx, non_blocking=True)
+        sim.find_constraints()
+        sim.compute_hessian_and_gradient()
+        sim.solve_system(t)
+        hp.copy_(sim.data_sol, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize(dev)
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    pk = fp64_peak(dev)
+    achieved = st['flops'] / (ms * 1e-3) / 1e12
+    line = {'metric': DIRECT_METRIC, 'value': 1e3 / ms, 'unit': 'solves/s', 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic', 'config': cfg, 'gpu_launches': int(launches),
+            'direct': {'fronts': st['fronts'], 'front_gb': st['front_doubles'] * 8e-9, 'factor_flops': st['flops'],
+                       'analyse_ms': st['analyse_ms'], 'contact_rows': int(sum(sim.counts)), 'step_of_first_contact': f,
+                       'agreement_with_pcg_1e-12': agree},
+            'roofline': {'kernel': 'whole direct solve (k_mf_update holds nearly all its flops)', 'bound': 'fp64',
+                         'achieved': achieved, 'peak': pk['tflops'], 'unit': 'TFLOP/s', 'frac': achieved / pk['tflops'],
+                         'traffic': None, 'peak_source': 'measured: ' + pk['how'],
+                         'note': 'dense factorisation flops of the fronts over the whole solve time (host analysis and '
+                                 'substitution included)'},
+            'clocks': clk.summary(),
+            'e2e': {'value': 1e3 / e2e_ms, 'unit': 'solves/s', 'h2d_bytes_per_step': int(hx.numel() * 8),
+                    'd2h_bytes_per_step': int(hp.numel() * 8)}}
+    if not args.no_cpu_baseline and rank == 0:
+        v, sample = cpu_solve(x_h, v_h, f)
+        line['cpu_baseline'] = {'value': v, 'unit': 'solves/s', 'cores': 1, 'kind': 'port', 'sample': sample}
+    sim.close()
+    _ = np
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def batch_cpu(scs, args, budget_s=20.0):

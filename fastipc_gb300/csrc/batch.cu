@@ -149,7 +149,7 @@ __global__ void k_fill_f64(int n, double* __restrict__ a, double v) {
 namespace fipc {
 
 struct BPCG {
-    PCGArgs m;                    // operands and vectors; m.part / m.sc / m.flag unused
+    PCGArgs m{};                  // operands and vectors; m.part / m.sc / m.flag unused
     int S, n_tiles, maxit, dry;   // dry: SpMV only (timing), no partials and no scalars
     const int* tile_scene;        // [n_tiles]
     const int* tile_row0;         // [n_tiles]
@@ -473,8 +473,10 @@ static void fill_tables(const fipc_ctx* c, BPCG& a) {
     a.part = c->bpcg_part.as<double>();
 }
 
-// block shape (rows per tile = threads per block) and persistent grid, chosen by timing the SpMV
-// on the live system: every candidate runs its SpMV without reductions, best of three launches
+// persistent grid of the batched PCG, chosen by timing the SpMV on the live system: every
+// candidate runs its SpMV without reductions, best of three launches.  The tile (rows per tile =
+// threads per block) stays at 128 rows: it sets the order of the per-scene sums, so choosing it by
+// timing would make the directions depend on the timing; the grid does not change any sum.
 static int autotune(fipc_ctx* c, BPCG a, cudaStream_t s) {
     int dev = 0, nsm = 152;
     cudaGetDevice(&dev);
@@ -482,7 +484,7 @@ static int autotune(fipc_ctx* c, BPCG a, cudaStream_t s) {
     cudaEvent_t e0, e1;
     FIPC_CUDA(cudaEventCreate(&e0));
     FIPC_CUDA(cudaEventCreate(&e1));
-    const int trs[3] = {64, 128, 256};
+    const int trs[1] = {128};
     const int mult[5] = {2, 4, 8, 16, 0};   // 0: one block per tile
     float best = 1e30f;
     int best_tr = 128, best_grid = 0;
@@ -661,6 +663,7 @@ extern "C" int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const in
 extern "C" int fipc_ctx_destroy(fipc_ctx* c);
 namespace fipc {
 int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h);
+void mg_free(fipc_ctx* c);
 double median_edge_inv(const double* x, const int* be, int e0, int e1, double fallback);
 }
 
@@ -723,6 +726,7 @@ int fipc_batch_create(fipc_ctx** out, int n_scenes, const int* vert_off, const i
     int st = fipc_ctx_create(&c, n_verts, n_tets, tets, x_rest, lam, mu, rho, n_bp, bp, n_be, be, n_bt, bt, dhat2, dt);
     if (st) return st;
     cs_setup(c, 0, nullptr, nullptr);   // the batched PCG preconditions with block-Jacobi
+    mg_free(c);
     // per-scene kappa (NEWTON_IPC.py:116-124, x10 at :943) and hash cell (:127-134)
     std::vector<double> mass(n_verts), kap(S), idx(S), hidx(S);
     if (cudaMemcpy(mass.data(), c->mass, 8ll * n_verts, cudaMemcpyDeviceToHost) != cudaSuccess) {

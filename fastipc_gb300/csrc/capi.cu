@@ -26,6 +26,8 @@ int launch_energy(const fipc_ctx* c, const double* x, const double* xt, const in
 int launch_absmax(int n, const double* p, double* part, double* out, cudaStream_t s);
 void free_batch(fipc_ctx* c);
 int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h);
+int mg_setup(fipc_ctx* c, double h);
+void mg_free(fipc_ctx* c);
 void cs_free(fipc_ctx* c);
 // 1 / median length of boundary edges [e0, e1) (fallback when there are none)
 double median_edge_inv(const double* x, const int* be, int e0, int e1, double fallback) {
@@ -71,6 +73,7 @@ void free_ctx(fipc_ctx* c) {
     c->pcg3_exec = nullptr;
     free_batch(c);
     cs_free(c);
+    mg_free(c);
     void* ptrs[] = {c->tets, c->bp, c->be, c->bt, c->dminv, c->vol, c->lam, c->mu, c->mass, c->x0, c->row_ptr, c->col_idx,
                     c->up_pos, c->up_tpos, c->up_row, c->up_cptr, c->up_contrib, c->vt_ptr, c->vt_list, c->elem_g, c->elem_H,
                     c->bsr_val, c->rhs, c->d_counts, c->diag_pos, c->sell_off, c->sell_col, c->row_len, c->bsr2sell,
@@ -310,6 +313,7 @@ int fipc_ctx_create(fipc_ctx** out, int n_verts, int n_tets, const int* tets, co
     }
     if (st == FIPC_OK) st = ensure_row_capacity(c, 4096);
     if (st == FIPC_OK) st = cs_setup(c, default_agg_rows(n_verts), row_ptr.data(), col_idx.data());
+    if (st == FIPC_OK) st = mg_setup(c, 0.0);
     if (st != FIPC_OK) {
         free_ctx(c);
         return FIPC_ERR_CUDA;
@@ -327,11 +331,21 @@ int fipc_ctx_destroy(fipc_ctx* c) {
 
 int fipc_ctx_set_preconditioner(fipc_ctx* c, int agg_rows) {
     if (!c || agg_rows < 0 || agg_rows % 128) return FIPC_ERR_ARGUMENT;
+    mg_free(c);   // an explicit choice of the one- or two-level preconditioner
     std::vector<int> rp(c->nV + 1), ci(c->nnzb);
     if (cudaMemcpy(rp.data(), c->row_ptr, 4ll * (c->nV + 1), cudaMemcpyDeviceToHost) != cudaSuccess ||
         cudaMemcpy(ci.data(), c->col_idx, 4ll * c->nnzb, cudaMemcpyDeviceToHost) != cudaSuccess)
         return FIPC_ERR_CUDA;
     return cs_setup(c, agg_rows, rp.data(), ci.data());
+}
+
+int fipc_ctx_set_multigrid(fipc_ctx* c, int on, double h) {
+    if (!c) return FIPC_ERR_ARGUMENT;
+    if (!on) {
+        mg_free(c);
+        return FIPC_OK;
+    }
+    return mg_setup(c, h);
 }
 
 int fipc_ctx_preconditioner(fipc_ctx* c, int* agg_rows, int* n_coarse) {

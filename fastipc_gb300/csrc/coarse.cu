@@ -273,7 +273,10 @@ __global__ void __launch_bounds__(PCG_THREADS) k_cs_prolong(PCGArgs a) {
 // ---------------------------------------------------------------- host side
 // aggregate pairs coupled by the static pattern (host, at context creation or on a change of
 // the aggregate size)
+void pcg_graph_reset(fipc_ctx* c);
+
 int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx_h) {
+    pcg_graph_reset(c);
     if (c->cs_pairs) cudaFree(c->cs_pairs);
     c->cs_pairs = nullptr;
     c->cs_agg_rows = 0;
@@ -299,11 +302,27 @@ int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx
     c->cs_agg_rows = agg_rows;
     c->cs_n_agg = na;
     c->cs_n_pairs = (int)keys.size();
+    // offsets from the rest shape until the next assembly sets them at its positions (any
+    // centre spans the same rigid-body modes, so the coarse space is valid either way)
+    if (c->cs_d.ensure(24ll * c->nV)) return FIPC_ERR_CUDA;
+    k_cs_offsets<<<c->cs_n_agg, CS_THREADS>>>(c->nV, c->cs_agg_rows, c->x0, c->cs_d.as<double>());
+    FIPC_LAUNCHED();
+    if (cudaDeviceSynchronize() != cudaSuccess) return FIPC_ERR_CUDA;
     return FIPC_OK;
 }
 
-// offsets from the aggregate centroids at the Newton iterate x (called by the assembly)
+int mg_offsets(fipc_ctx* c, const double* x, cudaStream_t s);
+
+// the blocked Gauss-Jordan inverse for other preconditioner levels (n a multiple of GJ_B)
+int cs_gauss_jordan(int n, double* A, double* buf, cudaStream_t s) { return launch_gauss_jordan(n, A, buf, s); }
+
+// offsets from the aggregate centroids at the Newton iterate x (called by the assembly), and the
+// multigrid hierarchy's when it is in use
 int cs_offsets(fipc_ctx* c, const double* x, cudaStream_t s) {
+    if (c->mg) {
+        const int st = mg_offsets(c, x, s);
+        if (st) return st;
+    }
     if (!c->cs_agg_rows) return FIPC_OK;
     if (c->cs_d.ensure(24ll * c->nV)) return FIPC_ERR_CUDA;
     k_cs_offsets<<<c->cs_n_agg, CS_THREADS, 0, s>>>(c->nV, c->cs_agg_rows, x, c->cs_d.as<double>());

@@ -128,6 +128,14 @@ struct fipc_ctx_impl {
     // single-scene PCG: a captured chunk of iterations and the kernel arguments it holds
     void* pcg3_exec = nullptr;
     std::vector<unsigned char> pcg3_sig;
+    // multigrid preconditioner of the PCG (mg_levels >= 2: in use, replacing the coarse space
+    // above); an MgState owned by the context
+    void* mg = nullptr;
+    int mg_levels = 0;
+    // the last direct solve: fronts, their storage (doubles), factorisation flops, host analysis time
+    int mf_fronts = 0;
+    long long mf_front_doubles = 0;
+    double mf_flops = 0.0, mf_analyse_ms = 0.0;
 };
 
 // scene lookup for the spatial hash: one scene (null table) or per-vertex scene ids with

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <climits>
 #include <vector>
 
@@ -353,8 +354,13 @@ int fipc_solve_system_direct(fipc_ctx* c, const unsigned char* fixed, double* so
     FIPC_CUDA(cudaMemcpyAsync(x0.data(), c->x0, 24ll * nV, cudaMemcpyDeviceToHost, s));
     FIPC_CUDA(cudaStreamSynchronize(s));
     MfPlan P;
+    const auto t_an = std::chrono::steady_clock::now();
     if (mf_analyse(nV, rp.data(), ci.data(), c_nnzb ? crp.data() : nullptr, c_nnzb ? cci.data() : nullptr, fx.data(), x0.data(), P))
         return FIPC_ERR_ARGUMENT;
+    c->mf_analyse_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_an).count();
+    c->mf_fronts = P.n_nodes;
+    c->mf_front_doubles = P.f_total;
+    c->mf_flops = P.flops;
     FIPC_CUDA(cudaMemsetAsync(sol, 0, 24ll * nV, s));
     if (nnz_h) {
         long long stored = 0;
@@ -474,6 +480,15 @@ int fipc_solve_system_direct(fipc_ctx* c, const unsigned char* fixed, double* so
     FIPC_CUDA(cudaMemcpyAsync(&bad, d.flag, sizeof(int), cudaMemcpyDeviceToHost, s));
     FIPC_CUDA(cudaStreamSynchronize(s));
     return bad ? FIPC_ERR_NONFINITE : FIPC_OK;
+}
+
+int fipc_direct_stats(const fipc_ctx* c, int* fronts_h, long long* front_doubles_h, double* flops_h, double* analyse_ms_h) {
+    if (!c) return FIPC_ERR_ARGUMENT;
+    if (fronts_h) *fronts_h = c->mf_fronts;
+    if (front_doubles_h) *front_doubles_h = c->mf_front_doubles;
+    if (flops_h) *flops_h = c->mf_flops;
+    if (analyse_ms_h) *analyse_ms_h = c->mf_analyse_ms;
+    return FIPC_OK;
 }
 
 }  // extern "C"

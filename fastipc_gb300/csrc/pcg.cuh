@@ -27,6 +27,35 @@ struct PCGArgs {
     int* cs_ticket;                  // [n_agg] blocks of the aggregate done (reset by its last block)
     const double* cs_ainv;           // inverse coarse matrix, row stride cs_ld
     int cs_n, cs_ld;                 // 6 n_agg; padded row stride
+    // multigrid preconditioner (mg non-null, host pointer): the update kernel writes the
+    // pre-smoothed z0 = w0 D^-1 r (stride 4) instead of u, and the V-cycle produces u
+    const struct MgArgs* mg;
+    double* mg_z0;
+    const double* mg_omega;          // [levels] smoother weights (device)
+};
+
+// one level >= 1 of the multigrid hierarchy (6 DOFs per node), as the V-cycle kernels see it
+struct MgLev {
+    int n;                           // nodes
+    const int *mem_ptr, *mem;        // members (finer-level ids) of each node
+    const int* agg_of;               // node of each finer-level node
+    const double* d;                 // [3 n_finer] offsets of the finer nodes from their node's centroid
+    const int *s_rp, *s_ci;          // static pattern, 6x6 blocks
+    const double* s_val;
+    const int *c_rp, *c_ci;          // contact pattern (c_rp null: none)
+    const double* c_val;
+    const double* minv;              // [36 n] block-Jacobi inverses
+    double *g, *z, *z2, *t;          // [6 n]: restricted residual, iterate, post-smoothed, residual
+};
+constexpr int MG_LEVELS_CAP = 8;
+struct MgArgs {
+    int levels;
+    MgLev L[MG_LEVELS_CAP];          // L[1 .. levels - 1]
+    double* z0;                      // [4 nV] level-0 iterate
+    double* t0;                      // [3 nV] level-0 residual
+    const double* omega;             // [levels]
+    const double* dense;             // coarsest inverse, row stride ld_dense
+    int n_dense, ld_dense;
 };
 enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
 constexpr int PCG_THREADS = 128;

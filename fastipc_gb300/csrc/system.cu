@@ -17,6 +17,8 @@
 #include <algorithm>
 
 #include <cub/cub.cuh>
+
+#include <vector>
 #include <cuda_runtime.h>
 
 #include "ctx.cuh"
@@ -346,7 +348,9 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_update(PCGArgs a) {
             a.s[q] = sn[d];
             a.x[q] = x[d] + alpha * pn[d];
             a.r[q] = rn[d];
-            a.u[4 * i + d] = M[3 * d] * rn[0] + M[3 * d + 1] * rn[1] + M[3 * d + 2] * rn[2];
+            const double z = M[3 * d] * rn[0] + M[3 * d + 1] * rn[1] + M[3 * d + 2] * rn[2];
+            if (a.mg_z0) a.mg_z0[4 * i + d] = a.mg_omega[0] * z;
+            else a.u[4 * i + d] = z;
         }
     }
     if (a.cs_blocks) block_restrict(a, i < a.nV, i, rn, d3);
@@ -373,6 +377,10 @@ int launch_barrier_rows(int type, int n, const int* rows, const double* x, const
 int cs_offsets(fipc_ctx* c, const double* x, cudaStream_t s);
 int cs_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t s);
 void cs_apply(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s);
+int mg_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t s);
+int mg_start(fipc_ctx* c, const PCGArgs& a, cudaStream_t s);
+void mg_vcycle(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s);
+int mg_launches_per_cycle(int levels);
 
 int contact_prepare(fipc_ctx* c, TypeTable* tt, int* nrows_out, long long* nent_out, cudaStream_t s);
 
@@ -501,13 +509,20 @@ int sell_to_bsr(fipc_ctx* c, double* out, cudaStream_t s) {
 // their first instruction, so a chunk overshoots by at most PCG3_CHUNK - 1 empty launches
 constexpr int PCG3_CHUNK = 32;
 
+// drops the captured PCG chunk (its kernels hold the preconditioner's buffers)
+void pcg_graph_reset(fipc_ctx* c) {
+    if (c->pcg3_exec) cudaGraphExecDestroy((cudaGraphExec_t)c->pcg3_exec);
+    c->pcg3_exec = nullptr;
+    c->pcg3_sig.clear();
+}
+
 // a graph of PCG3_CHUNK iterations (SpMV, update, coarse correction) for these kernel
 // arguments, captured on the context's private stream and replayed on the caller's; reused
 // while the arguments (buffers, sizes) stay the same; false when capture is unavailable
 static bool pcg3_graph(fipc_ctx* c, const PCGArgs& a) {
-    const unsigned char* sig = reinterpret_cast<const unsigned char*>(&a);
-    if (c->pcg3_exec && c->pcg3_sig.size() == sizeof(PCGArgs) && std::equal(sig, sig + sizeof(PCGArgs), c->pcg3_sig.begin()))
-        return true;
+    std::vector<unsigned char> sig(reinterpret_cast<const unsigned char*>(&a), reinterpret_cast<const unsigned char*>(&a) + sizeof(PCGArgs));
+    if (a.mg) sig.insert(sig.end(), reinterpret_cast<const unsigned char*>(a.mg), reinterpret_cast<const unsigned char*>(a.mg) + sizeof(MgArgs));
+    if (c->pcg3_exec && c->pcg3_sig == sig) return true;
     if (c->pcg3_exec) cudaGraphExecDestroy((cudaGraphExec_t)c->pcg3_exec);
     c->pcg3_exec = nullptr;
     c->pcg3_sig.clear();
@@ -523,7 +538,8 @@ static bool pcg3_graph(fipc_ctx* c, const PCGArgs& a) {
     for (int k = 0; k < PCG3_CHUNK; ++k) {
         k_pcg_spmv<<<nb, PCG_THREADS, 0, cs>>>(a);
         k_pcg_update<<<nb, PCG_THREADS, 0, cs>>>(a);
-        if (a.cs_blocks) cs_apply(c, a, cs);
+        if (a.mg) mg_vcycle(c, a, cs);
+        else if (a.cs_blocks) cs_apply(c, a, cs);
     }
     g_launches.store(counted);
     cudaGraph_t g = nullptr;
@@ -539,7 +555,7 @@ static bool pcg3_graph(fipc_ctx* c, const PCGArgs& a) {
         return false;
     }
     c->pcg3_exec = ex;
-    c->pcg3_sig.assign(sig, sig + sizeof(PCGArgs));
+    c->pcg3_sig = sig;
     return true;
 }
 
@@ -554,7 +570,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     if (c->c_nnzb == 0 && (c->c_rowptr.ensure(4ll * (c->nV + 1)) || cudaMemsetAsync(c->c_rowptr.p, 0, 4ll * (c->nV + 1), s)))
         return FIPC_ERR_CUDA;
     if (c->c_val.ensure(72) || c->c_col.ensure(4)) return FIPC_ERR_CUDA;
-    PCGArgs a;
+    PCGArgs a{};
     a.nV = c->nV;
     a.soff = c->sell_off;
     a.scol = c->sell_col;
@@ -577,8 +593,9 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     a.sc = a.part + 3 * nb;
     a.flag = (int*)(c->scal.as<char>() + 48);
     FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 4 * sizeof(int), s));
-    int st = cs_prepare(c, fixed, a, s);
+    int st = c->mg ? mg_prepare(c, fixed, a, s) : cs_prepare(c, fixed, a, s);
     if (st) return st;
+    if (a.mg) a.cs_blocks = 0;
     // traffic model per launch: matrix blocks and column ids once (padding slots included),
     // row data, the gathered vector once, w written, r read
     const double slots = 32.0 * (double)c->n_slots, nv = (double)c->nV, cn = (double)c->c_nnzb;
@@ -588,14 +605,19 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     const double upd_flops = nv * 36.0;
     k_pcg_start<<<nb, PCG_THREADS, 0, s>>>(a, c->rhs, rtol);
     FIPC_LAUNCHED();
-    if (a.cs_blocks) cs_apply(c, a, s);
+    if (a.mg) {
+        st = mg_start(c, a, s);
+        if (st) return st;
+    } else if (a.cs_blocks) {
+        cs_apply(c, a, s);
+    }
     int h_flag[2] = {0, 0};
     // per-launch timing of the SpMV or the update needs plain launches; otherwise whole chunks of
     // iterations replay from a captured graph (one launch per chunk instead of four per iteration)
     const int pk = profile_kernel();
     const bool timed = pk == PK_PCG_SPMV || pk == PK_PCG_UPDATE;
     const bool graph = !timed && maxit >= PCG3_CHUNK && pcg3_graph(c, a);
-    const int per_iter = a.cs_blocks ? 4 : 2;
+    const int per_iter = a.mg ? 2 + mg_launches_per_cycle(c->mg_levels) : (a.cs_blocks ? 4 : 2);
     int k0 = 0;
     while (k0 < maxit) {
         if (graph && k0 + PCG3_CHUNK <= maxit) {
@@ -615,7 +637,8 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
                     k_pcg_update<<<nb, PCG_THREADS, 0, s>>>(a);
                 }
                 FIPC_LAUNCHED();
-                if (a.cs_blocks) cs_apply(c, a, s);
+                if (a.mg) mg_vcycle(c, a, s);
+                else if (a.cs_blocks) cs_apply(c, a, s);
             }
             k0 = k1;
         }

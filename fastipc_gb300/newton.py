@@ -146,8 +146,19 @@ class NewtonIPC:
 
     def set_preconditioner(self, agg_rows):
         """0: block-Jacobi PCG; a multiple of 128: add the rigid-body coarse space of every run of
-        agg_rows consecutive vertices (the default at creation)."""
+        agg_rows consecutive vertices.  Either switches the multigrid preconditioner off."""
         check(N.lib().fipc_ctx_set_preconditioner(self.ctx, int(agg_rows)), 'fipc_ctx_set_preconditioner')
+
+    def set_multigrid(self, on=True, h=0.0):
+        """The multigrid preconditioner (the default for scenes of at least 1000 vertices): on or
+        off; h is the first aggregation box's cell (0: the spatial hash's)."""
+        check(N.lib().fipc_ctx_set_multigrid(self.ctx, int(bool(on)), D(h)), 'fipc_ctx_set_multigrid')
+
+    def multigrid(self):
+        """Levels of the multigrid hierarchy in use (0: off) and nodes per level."""
+        lv, nodes = ctypes.c_int(), (ctypes.c_int * 8)()
+        check(N.lib().fipc_ctx_multigrid(self.ctx, ctypes.byref(lv), nodes), 'fipc_ctx_multigrid')
+        return {'levels': lv.value, 'nodes': [nodes[k] for k in range(lv.value)]}
 
     def preconditioner(self):
         a, n = ctypes.c_int(), ctypes.c_int()
@@ -258,6 +269,14 @@ class NewtonIPC:
         check(N.lib().fipc_solve_system_direct(self.ctx, dptr(self.fixed, torch.uint8), dptr(self.data_sol, F64), None, self._s()),
               'solve_system_direct')
         self.direct_solves += 1
+
+    def direct_stats(self):
+        """The last direct solve: fronts, front storage (doubles), factorisation flops and the host
+        analysis time (ms)."""
+        nf, nd, fl, ms = ctypes.c_int(), ctypes.c_longlong(), D(), D()
+        check(N.lib().fipc_direct_stats(self.ctx, ctypes.byref(nf), ctypes.byref(nd), ctypes.byref(fl), ctypes.byref(ms)),
+              'fipc_direct_stats')
+        return {'fronts': nf.value, 'front_doubles': nd.value, 'flops': fl.value, 'analyse_ms': ms.value}
 
     def output_residual(self):
         r = D()

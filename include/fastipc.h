@@ -82,10 +82,21 @@ int fipc_ctx_mass(fipc_ctx* ctx, double* mass_h);
 int fipc_ctx_set_x0(fipc_ctx* ctx, const double* x0, void* stream);
 /* Preconditioner of fipc_solve_system: agg_rows = 0 selects block-Jacobi; a positive multiple of
  * 128 adds the coarse correction on the six rigid-body modes of every run of agg_rows
- * consecutive vertices (at most 1024 runs).  The default at creation is 2048 (or larger, so
- * that there are at most 512 runs).  The solution satisfies the same tolerance either way. */
+ * consecutive vertices (at most 1024 runs).  Either switches the multigrid preconditioner below
+ * off.  The solution satisfies the same tolerance with every preconditioner. */
 int fipc_ctx_set_preconditioner(fipc_ctx* ctx, int agg_rows);
 int fipc_ctx_preconditioner(fipc_ctx* ctx, int* agg_rows, int* n_coarse);
+/* Multigrid preconditioner of fipc_solve_system (no counterpart in the reference, which solves
+ * directly): geometric aggregation of the rest shape into boxes (the first three cells h wide,
+ * each coarser level's twice the last, never across two bodies), six rigid-body modes per
+ * aggregate, Galerkin coarse matrices rebuilt every Newton iteration (contact blocks included),
+ * one symmetric V(1,1)-cycle with damped block-Jacobi smoothing per PCG iteration, dense inverse
+ * at the coarsest level.  When in use it replaces the coarse correction selected above.  on = 0
+ * switches it off; h <= 0 takes the spatial hash's cell.  Created on by default for
+ * single-scene contexts of at least 1000 vertices.  fipc_ctx_multigrid: levels in use (0:
+ * off) and nodes per level (nodes_h: 8 ints, may be NULL). */
+int fipc_ctx_set_multigrid(fipc_ctx* ctx, int on, double h);
+int fipc_ctx_multigrid(fipc_ctx* ctx, int* levels, int* nodes_h);
 /* In-place inverse of a dense SPD matrix on the device (n a multiple of 32, row-major; work: 1024
  * + 64 n doubles): the blocked Gauss-Jordan used for the coarse matrix, one cooperative launch. */
 int fipc_dense_spd_inverse(int n, double* a, double* work, void* stream);
@@ -117,6 +128,9 @@ int fipc_solve_system(fipc_ctx* ctx, const unsigned char* fixed, double rtol, in
  * 1 when its fronts do not fit in free device memory.  nnz_h (may be NULL): entries stored in
  * the factor's fronts (lower triangles), saturated at INT_MAX. */
 int fipc_solve_system_direct(fipc_ctx* ctx, const unsigned char* fixed, double* sol, int* nnz_h, void* stream);
+/* the last direct solve (no counterpart in the reference): fronts of its assembly tree, doubles
+ * of front storage, dense factorisation flops, host analysis time in ms (each may be NULL) */
+int fipc_direct_stats(const fipc_ctx* ctx, int* fronts_h, long long* front_doubles_h, double* flops_h, double* analyse_ms_h);
 int fipc_output_residual(fipc_ctx* ctx, const double* sol, double* res_h, void* stream);
 
 /* compute_energy, NEWTON_IPC.py:514-542, over the lists of the last find_constraints */

@@ -5,8 +5,8 @@ Bars, from one state: kappa, hash cell and constraint lists identical; per-scene
 relative; PCG directions 1e-8 relative at rtol 1e-12 (different summation order); CCD steps
 1e-6.  Over whole steps the line search compares energies that agree to rounding, and near
 convergence E and E0 agree to about as many digits, so the two runs may halve differently:
-they take the same Newton iteration counts and end within the Newton tolerance
-(|p|inf < 1e-2 dt = 1e-4 m) of each other."""
+their Newton iteration counts agree within one per step and they end within the Newton
+tolerance (|p|inf < 1e-2 dt = 1e-4 m) of each other."""
 import numpy as np
 import pytest
 import torch
@@ -111,13 +111,17 @@ def test_inactive_scene_gets_zero_direction(pair):
 
 
 def test_full_steps_match_single_scenes():
+    """Whole steps: the single scenes run block-Jacobi PCG, as the batch does.  The two sides sum
+    in different orders, and a Newton iteration whose |p|inf lands within rounding of the
+    tolerance can end the loop on one side and not the other; each step may therefore differ by
+    one Newton iteration, and the positions agree within the Newton tolerance."""
     sc = small_scenes()
     batch = BatchNewtonIPC(sc, pcg_rtol=1e-12)
-    singles = [NewtonIPC(s, pcg_rtol=1e-12) for s in sc]
+    singles = [NewtonIPC(s, pcg_rtol=1e-12, coarse_agg=0) for s in sc]
     for f in range(4):
         its = batch.step(f)
         for s, one in enumerate(singles):
-            assert one.step(f) == its[s]
+            assert abs(one.step(f) - int(its[s])) <= 1, (s, f)
     for s, one in enumerate(singles):
         xb = batch.x[batch.scene_slice(s)]
         ext = (one.x.max(0).values - one.x.min(0).values).max().item()

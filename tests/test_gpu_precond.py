@@ -1,6 +1,7 @@
 """The two-level PCG preconditioner (block-Jacobi + rigid-body coarse space) on the GB300: the
 Newton direction is the same as with block-Jacobi alone (both solve the reference's system to
-the tolerance), with fewer iterations on a long bar.
+the tolerance), with fewer iterations on a long bar.  (The multigrid preconditioner, the default,
+is checked in test_gpu_multigrid.py; set_preconditioner switches it off.)
 
 Bars: directions within 1e-8 relative at rtol 1e-12; at least 2x fewer PCG iterations."""
 import numpy as np
@@ -30,7 +31,10 @@ def solve(sim, agg):
     return sim.data_sol.clone(), sim.pcg_iters[-1]
 
 
-def test_default_is_two_level(bar):
+def test_default_is_multigrid_with_two_level_configured(bar):
+    """Multigrid is in use at creation; the two-level coarse space stays configured (2048-vertex
+    runs) and takes over when set_preconditioner selects it."""
+    assert bar.multigrid()['levels'] >= 2
     p = bar.preconditioner()
     assert p['agg_rows'] == 2048 and p['coarse_dofs'] == 6 * ((bar.nV + 2047) // 2048)
 
