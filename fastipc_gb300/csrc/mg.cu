@@ -58,13 +58,13 @@ struct MgLevelBufs {
 struct MgState {
     MgPlan plan;
     std::vector<MgLevelBufs> B;
-    DBuf dense, gj_buf, omega, t0, z0;
+    DBuf dense, gj_buf, omega, t0, z0, terms;
     int n_dense = 0, ld_dense = 0;
     bool contact_empty = true;                       // the per-level contact patterns are empty
     MgArgs args{};                                   // kernel arguments of the V-cycle
     ~MgState() {
         for (MgLevelBufs& b : B) b.release();
-        DBuf* all[] = {&dense, &gj_buf, &omega, &t0, &z0};
+        DBuf* all[] = {&dense, &gj_buf, &omega, &t0, &z0, &terms};
         for (DBuf* b : all) b->release();
     }
 };
@@ -173,6 +173,46 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_galerkin(int nnz, const int* 
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) out[36 * (size_t)b + e] = v;
+    }
+}
+
+// Level 1 from the system's 3x3 blocks, in two passes (fewer registers per thread than one warp
+// per coarse block, so far more contributions are in flight): every contribution's 6x6 product
+// P_i^T A_ij P_j into terms [contribution][36] (zeros for Dirichlet vertices), then every coarse
+// block sums its contiguous run of terms in list order, one lane per entry.
+template <bool SELL>
+__global__ void __launch_bounds__(MG_THREADS) k_mg_gal_terms(int nq, const int* __restrict__ src, const int* __restrict__ srow,
+                                                             const int* __restrict__ scol, const double* __restrict__ fval,
+                                                             const int* __restrict__ bsr2sell, const unsigned char* __restrict__ fixed,
+                                                             const double* __restrict__ d, double* __restrict__ terms) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nq) return;
+    double C[36];
+#pragma unroll
+    for (int e = 0; e < 36; ++e) C[e] = 0.0;
+    const int i = srow[q], j = scol[q];
+    if (!fixed[i] && !fixed[j]) {
+        const double di[3] = {d[3 * (size_t)i], d[3 * (size_t)i + 1], d[3 * (size_t)i + 2]};
+        const double dj[3] = {d[3 * (size_t)j], d[3 * (size_t)j + 1], d[3 * (size_t)j + 2]};
+        if (SELL) {
+            const int ps = bsr2sell[src[q]];
+            gal_add<3>(C, fval + (size_t)(ps >> 5) * 288 + (ps & 31), 32, di, dj);
+        } else {
+            gal_add<3>(C, fval + 9 * (size_t)src[q], 1, di, dj);
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < 36; ++e) terms[36 * (size_t)q + e] = C[e];
+}
+
+__global__ void __launch_bounds__(MG_THREADS) k_mg_gal_sum(int nnz, const int* __restrict__ cp, const double* __restrict__ terms,
+                                                           double* __restrict__ out) {
+    const int b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+    if (b >= nnz) return;
+    for (int e = lane; e < 36; e += 32) {
+        double t = 0.0;
+        for (int q = cp[b]; q < cp[b + 1]; ++q) t += terms[36 * (size_t)q + e];
+        out[36 * (size_t)b + e] = t;
     }
 }
 
@@ -646,14 +686,21 @@ int mg_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
         const double* d = b.d.as<double>();
         const int ns = p.S.nnz(), ncn = p.C.nnz();
         if (l == 1) {
-            if (ns)
-                k_mg_galerkin<3, true><<<nblk_m(32ll * ns, MG_THREADS), MG_THREADS, 0, s>>>(
-                    ns, b.s_cp.as<int>(), b.s_src.as<int>(), b.s_row.as<int>(), b.s_col.as<int>(), c->sell_val, c->bsr2sell, fixed, d,
-                    b.s_val.as<double>());
-            if (ncn)
-                k_mg_galerkin<3, false><<<nblk_m(32ll * ncn, MG_THREADS), MG_THREADS, 0, s>>>(
-                    ncn, b.c_cp.as<int>(), b.c_src.as<int>(), b.c_row.as<int>(), b.c_col.as<int>(), c->c_val.as<double>(), nullptr,
-                    fixed, d, b.c_val.as<double>());
+            const int nqs = (int)p.S.src.size(), nqc = (int)p.C.src.size();
+            if (M->terms.ensure(288ull * (nqs > nqc ? nqs : nqc) + 8)) return FIPC_ERR_CUDA;
+            double* terms = M->terms.as<double>();
+            if (ns) {
+                k_mg_gal_terms<true><<<nblk_m(nqs, MG_THREADS), MG_THREADS, 0, s>>>(
+                    nqs, b.s_src.as<int>(), b.s_row.as<int>(), b.s_col.as<int>(), c->sell_val, c->bsr2sell, fixed, d, terms);
+                k_mg_gal_sum<<<nblk_m(32ll * ns, MG_THREADS), MG_THREADS, 0, s>>>(ns, b.s_cp.as<int>(), terms, b.s_val.as<double>());
+                g_launches.fetch_add(1, std::memory_order_relaxed);
+            }
+            if (ncn) {
+                k_mg_gal_terms<false><<<nblk_m(nqc, MG_THREADS), MG_THREADS, 0, s>>>(
+                    nqc, b.c_src.as<int>(), b.c_row.as<int>(), b.c_col.as<int>(), c->c_val.as<double>(), nullptr, fixed, d, terms);
+                k_mg_gal_sum<<<nblk_m(32ll * ncn, MG_THREADS), MG_THREADS, 0, s>>>(ncn, b.c_cp.as<int>(), terms, b.c_val.as<double>());
+                g_launches.fetch_add(1, std::memory_order_relaxed);
+            }
         } else {
             const MgLevelBufs& f = M->B[l - 1];
             if (ns)

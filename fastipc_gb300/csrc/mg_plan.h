@@ -25,7 +25,7 @@
 namespace fipc {
 
 constexpr int MG_MAX_LEVELS = 8;
-constexpr int MG_COARSEST = 48;        // aggregate until at most this many nodes remain (the dense coarsest: <= 288 DOFs)
+constexpr int MG_COARSEST = 160;       // aggregate until at most this many nodes remain (the dense coarsest: <= 960 DOFs)
 
 // a block pattern (CSR over nodes, both triangles) with its Galerkin contribution lists: block
 // s of this pattern sums the source blocks src[con_ptr[s] .. con_ptr[s + 1]) of the finer level
