@@ -48,6 +48,8 @@ def parse():
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--precond', default='multigrid', choices=['multigrid', 'two-level'],
                     help='PCG preconditioner of the bar, lattice and cube workloads')
+    ap.add_argument('--mg-smoothing', default='fp32', choices=['fp64', 'fp32'],
+                    help="precision of the multigrid V-cycle's two level-0 smoothing products")
     ap.add_argument('--cpu-sample-pcg', type=int, default=100000)
     ap.add_argument('--workload', default='bar', choices=['bar', 'batch', 'lattice', 'cubes', 'stack2d', 'admm', 'direct'],
                     help='bar: the 960k-tet twisted bar (headline); batch: 512 independent cube stacks in one context; '
@@ -327,6 +329,7 @@ def main():
     sim = NewtonIPC(scene, device=dev, pcg_rtol=args.pcg_rtol, pcg_warm_start=bool(args.warm_start))
     if args.precond == 'two-level':
         sim.set_preconditioner(2048)
+    sim.set_multigrid_fp32(args.mg_smoothing == 'fp32')
     mg = sim.multigrid()
 
     def barrier():
@@ -427,7 +430,8 @@ def main():
         if note:
             roof['traffic_note'] = note
         cfg = workload(args)
-        cfg['preconditioner'] = (f'multigrid V(1,1), {mg["levels"]} levels of {mg["nodes"]} nodes' if mg['levels']
+        cfg['preconditioner'] = (f'multigrid V(1,1), {mg["levels"]} levels of {mg["nodes"]} nodes, '
+                                 f'{args.mg_smoothing.upper()} level-0 smoothing products' if mg['levels']
                                  else 'two-level additive (rigid-body modes of 2048-vertex runs)')
         out = {'metric': metric(args), 'value': value, 'unit': 'steps/s', 'n_gpus': world, 'steps': args.steps,
                'warmup': args.warmup, 'ms_per_step': ms_max / args.steps, 'higher_is_better': True, 'scaling': 'weak',

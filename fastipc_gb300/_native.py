@@ -25,7 +25,7 @@ EXPORTS = [
     'fipc_compute_energy_noalloc', 'fipc_mlp_param_count', 'fipc_mlp_forward', 'fipc_mlp_backward', 'fipc_mlp_mse',
     'fipc_mlp_adam', 'fipc_mlp_features', 'fipc_batch_create', 'fipc_batch_params', 'fipc_batch_compute_energy',
     'fipc_batch_output_residual', 'fipc_batch_step_size', 'fipc_batch_check_collision', 'fipc_batch_apply_sol',
-    'fipc_batch_solve_system', 'fipc_batch_pcg_shape', 'fipc_ctx_set_preconditioner', 'fipc_ctx_preconditioner', 'fipc_ctx_set_multigrid', 'fipc_ctx_multigrid', 'fipc_mlp_smooth', 'fipc_dense_spd_inverse',
+    'fipc_batch_solve_system', 'fipc_batch_pcg_shape', 'fipc_ctx_set_preconditioner', 'fipc_ctx_preconditioner', 'fipc_ctx_set_multigrid', 'fipc_ctx_multigrid', 'fipc_ctx_set_multigrid_fp32', 'fipc_mlp_smooth', 'fipc_dense_spd_inverse',
     'fipc_write_obj', 'fipc_solve_system_direct', 'fipc_direct_stats', 'fipc_admm_init', 'fipc_admm_reuse', 'fipc_admm_global', 'fipc_admm_local',
     'fipc_admm_dual', 'fipc2d_ctx_create', 'fipc2d_ctx_destroy', 'fipc2d_ctx_params', 'fipc2d_ctx_set_kappa', 'fipc2d_ctx_mass',
     'fipc2d_compute_xn_and_xtilde', 'fipc2d_move_nodes', 'fipc2d_apply_sol', 'fipc2d_compute_v', 'fipc2d_elements',

@@ -367,6 +367,41 @@ __global__ void __launch_bounds__(128) k_find_ee(int nbe, const int* __restrict_
 }
 
 // ---------------------------------------------------------------- CCD step filter
+// Pairs that pass the additive bound go to the exact interval test through a compacted list
+// instead of running it in the candidate loop, where one lane's exact test would hold its whole
+// warp (the candidate loops are divergent: lanes run different cells and candidates).  The
+// minimum over pairs does not depend on where a pair's toc is computed.
+struct CcdWork {
+    int a, b, slot, pad;   // point-triangle: vertex, triangle; edge-edge: edge, edge; filter slot
+    double d2, lb;         // current squared distance, additive lower bound
+};
+struct CcdList {
+    CcdWork* w;            // [2 cap]: point-triangle pairs, then edge-edge pairs
+    int* count;            // [2] pushes (may exceed cap: the lanes past it test inline)
+    int cap;
+};
+
+// the exact tests out of line, for the candidate loops' overflow path (keeps their registers low)
+__device__ __noinline__ double pt_exact_call(v3 P, v3 A, v3 B, v3 C, v3 dP, v3 dA, v3 dB, v3 dC, double eta, double d2, double lb) {
+    return pt_ccd_exact(P, A, B, C, dP, dA, dB, dC, eta, d2, lb);
+}
+__device__ __noinline__ double ee_exact_call(v3 A0, v3 A1, v3 B0, v3 B1, v3 dA0, v3 dA1, v3 dB0, v3 dB1, double eta, double d2,
+                                             double lb) {
+    return ee_ccd_exact(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2, lb);
+}
+
+// appends e for every calling lane (one atomic per coalesced group); false when the list is full
+__device__ __forceinline__ bool ccd_push(CcdWork* w, int* count, int cap, const CcdWork& e) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(count, (int)g.size());
+    base = g.shfl(base, 0);
+    const int k = base + (int)g.thread_rank();
+    if (k >= cap) return false;
+    w[k] = e;
+    return true;
+}
+
 __device__ __forceinline__ void atomic_min_pos(unsigned long long* slot, double v) {
     if (v >= 0.0) atomicMin(slot, (unsigned long long)__double_as_longlong(v));
 }
@@ -374,7 +409,7 @@ __device__ __forceinline__ void atomic_min_pos(unsigned long long* slot, double 
 // compute_filter_3D_PT (NEWTON_IPC.py:377-406): triangles query their moving bbox
 __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__ bt, const int* __restrict__ bp,
                                                 const double* __restrict__ x, const double* __restrict__ p, double dh, SceneGeo g,
-                                                double eta, GridView gv, CandView cv, unsigned long long* __restrict__ alpha) {
+                                                double eta, GridView gv, CandView cv, CcdList L, unsigned long long* __restrict__ alpha) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nbt) return;
     if (g.big_tri && g.big_tri[i]) return;
@@ -404,7 +439,11 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
                     const v3 P = ld3(x, pp), dP = ld3(p, pp);
                     if (!pt_aabb_moving(P, A, B, C, dP, dA, dB, dC, dh)) continue;
                     const double d2 = pt_dist2(P, A, B, C);
-                    atomic_min_pos(alpha + (g.vscene ? sc : 0), pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, d2));
+                    double lb;
+                    if (!pt_needs_exact(dP, dA, dB, dC, eta, d2, &lb)) continue;
+                    const int slot = g.vscene ? sc : 0;
+                    if (!ccd_push(L.w, L.count, L.cap, CcdWork{pp, i, slot, 0, d2, lb}))
+                        atomic_min_pos(alpha + slot, pt_exact_call(P, A, B, C, dP, dA, dB, dC, eta, d2, lb));
                 }
             }
 }
@@ -412,7 +451,7 @@ __global__ void __launch_bounds__(128) k_ccd_pt(int nbt, const int* __restrict__
 // compute_filter_3D_EE (NEWTON_IPC.py:409-440): edges query moving bbox +- dh
 __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__ be, const double* __restrict__ x,
                                                 const double* __restrict__ p, double dh, SceneGeo g, double eta,
-                                                GridView gv, CandView cv, unsigned long long* __restrict__ alpha) {
+                                                GridView gv, CandView cv, CcdList L, unsigned long long* __restrict__ alpha) {
     // QG lanes per query edge share the candidates of each cell
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) / QG, lane = threadIdx.x % QG;
     if (i >= nbe) return;
@@ -442,9 +481,40 @@ __global__ void __launch_bounds__(128) k_ccd_ee(int nbe, const int* __restrict__
                     const v3 B0 = ld3(x, b0), B1 = ld3(x, b1), dB0 = ld3(p, b0), dB1 = ld3(p, b1);
                     if (!ee_aabb_moving(A0, A1, B0, B1, dA0, dA1, dB0, dB1, dh)) continue;
                     const double d2 = ee_dist2(A0, A1, B0, B1);
-                    atomic_min_pos(alpha + (g.vscene ? sc : 0), ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2));
+                    double lb;
+                    if (!ee_needs_exact(dA0, dA1, dB0, dB1, eta, d2, &lb)) continue;
+                    const int slot = g.vscene ? sc : 0;
+                    if (!ccd_push(L.w + L.cap, L.count + 1, L.cap, CcdWork{i, j, slot, 0, d2, lb}))
+                        atomic_min_pos(alpha + slot, ee_exact_call(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2, lb));
                 }
             }
+}
+
+// the exact tests of the listed pairs, one thread per pair
+__global__ void __launch_bounds__(128) k_ccd_pt_exact(const int* __restrict__ bt, const double* __restrict__ x,
+                                                      const double* __restrict__ p, double eta, CcdList L,
+                                                      unsigned long long* __restrict__ alpha) {
+    const int n = min(L.count[0], L.cap);
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const CcdWork e = L.w[k];
+        const int t0 = bt[3 * e.b], t1 = bt[3 * e.b + 1], t2 = bt[3 * e.b + 2];
+        const v3 P = ld3(x, e.a), dP = ld3(p, e.a);
+        const v3 A = ld3(x, t0), B = ld3(x, t1), C = ld3(x, t2), dA = ld3(p, t0), dB = ld3(p, t1), dC = ld3(p, t2);
+        atomic_min_pos(alpha + e.slot, pt_ccd_exact(P, A, B, C, dP, dA, dB, dC, eta, e.d2, e.lb));
+    }
+}
+__global__ void __launch_bounds__(128) k_ccd_ee_exact(const int* __restrict__ be, const double* __restrict__ x,
+                                                      const double* __restrict__ p, double eta, CcdList L,
+                                                      unsigned long long* __restrict__ alpha) {
+    const int n = min(L.count[1], L.cap);
+    const CcdWork* w = L.w + L.cap;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const CcdWork e = w[k];
+        const int a0 = be[2 * e.a], a1 = be[2 * e.a + 1], b0 = be[2 * e.b], b1 = be[2 * e.b + 1];
+        const v3 A0 = ld3(x, a0), A1 = ld3(x, a1), B0 = ld3(x, b0), B1 = ld3(x, b1);
+        const v3 dA0 = ld3(p, a0), dA1 = ld3(p, a1), dB0 = ld3(p, b0), dB1 = ld3(p, b1);
+        atomic_min_pos(alpha + e.slot, ee_ccd_exact(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, e.d2, e.lb));
+    }
 }
 
 // compute_filter_3D_inversion_free (NEWTON_IPC.py:443-453)
@@ -456,6 +526,7 @@ __global__ void __launch_bounds__(128) k_ccd_inversion(int nT, const int4* __res
     const int4 t = tets[e];
     const v3 X[4] = {ld3(x, t.x), ld3(x, t.y), ld3(x, t.z), ld3(x, t.w)};
     const v3 P[4] = {ld3(p, t.x), ld3(p, t.y), ld3(p, t.z), ld3(p, t.w)};
+    if (inversion_cannot_flip(X, P, eta)) return;
     atomic_min_pos(alpha + (g.vscene ? g.scene(t.x) : 0), inversion_free_step(X, P, eta));
 }
 
@@ -590,7 +661,8 @@ __global__ void k_ccd_pt_big(BigArgs b, const double* __restrict__ x, const doub
             if (pp == t0 || pp == t1 || pp == t2) continue;
             const v3 P = ld3(x, pp), dP = ld3(p, pp);
             if (!pt_aabb_moving(P, A, B, C, dP, dA, dB, dC, dh)) continue;
-            atomic_min_pos(alpha + (g.vscene ? sc : 0), pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, pt_dist2(P, A, B, C)));
+            const double d2 = pt_dist2(P, A, B, C);
+            atomic_min_pos(alpha + (g.vscene ? sc : 0), pt_ccd(P, A, B, C, dP, dA, dB, dC, eta, d2));
         }
     }
 }
@@ -610,7 +682,8 @@ __global__ void k_ccd_ee_big(BigArgs b, const double* __restrict__ x, const doub
             const v3 A0 = ld3(x, a0), A1 = ld3(x, a1), B0 = ld3(x, b0), B1 = ld3(x, b1);
             const v3 dA0 = ld3(p, a0), dA1 = ld3(p, a1), dB0 = ld3(p, b0), dB1 = ld3(p, b1);
             if (!ee_aabb_moving(A0, A1, B0, B1, dA0, dA1, dB0, dB1, dh)) continue;
-            atomic_min_pos(alpha + (g.vscene ? sc : 0), ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, ee_dist2(A0, A1, B0, B1)));
+            const double d2 = ee_dist2(A0, A1, B0, B1);
+            atomic_min_pos(alpha + (g.vscene ? sc : 0), ee_ccd(A0, A1, B0, B1, dA0, dA1, dB0, dB1, eta, d2));
         }
     }
 }
@@ -918,11 +991,23 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     BigArgs bg;
     int st = big_prepare(c, x, p, &sg, &bg, s);
     if (st) return st;
+    CcdList L;
+    {
+        long long cap = 65536ll + c->nBE + c->nBT;
+        if (cap > (1ll << 21)) cap = 1ll << 21;
+        if (c->ccd_work.ensure(256 + 2 * cap * sizeof(CcdWork))) return FIPC_ERR_CUDA;
+        L.count = c->ccd_work.as<int>();
+        L.w = reinterpret_cast<CcdWork*>(c->ccd_work.as<char>() + 256);
+        L.cap = (int)cap;
+        FIPC_CUDA(cudaMemsetAsync(L.count, 0, 2 * sizeof(int), s));
+    }
     st = build_grid(c, c->gp, 2, c->nBP, c->bp, x, p, sg, s);
     if (st) return st;
     if (c->gp.n_entries > 0 && c->nBT > 0) {
         k_ccd_pt<<<nblk(c->nBT, 128), 128, 0, s>>>(c->nBT, c->bt, c->bp, x, p, c->dhat, sg, eta,
-                                                    view(c->gp), cands(c->gp), slot);
+                                                    view(c->gp), cands(c->gp), L, slot);
+        FIPC_LAUNCHED();
+        k_ccd_pt_exact<<<4 * BIG_GRID, 128, 0, s>>>(c->bt, x, p, eta, L, slot);
         FIPC_LAUNCHED();
     }
     if (c->nBT > 0 && c->nBP > 0) {
@@ -933,7 +1018,9 @@ int ccd_launch(fipc_ctx* c, const double* x, const double* p, double eta, bool i
     if (st) return st;
     if (c->ge.n_entries > 0) {
         k_ccd_ee<<<nblk((long long)QG * c->nBE, 128), 128, 0, s>>>(c->nBE, c->be, x, p, c->dhat, sg, eta, view(c->ge), cands(c->ge),
-                                                                   slot);
+                                                                   L, slot);
+        FIPC_LAUNCHED();
+        k_ccd_ee_exact<<<4 * BIG_GRID, 128, 0, s>>>(c->be, x, p, eta, L, slot);
         FIPC_LAUNCHED();
     }
     if (c->nBE > 1) {

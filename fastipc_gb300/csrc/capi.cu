@@ -82,7 +82,7 @@ void free_ctx(fipc_ctx* c) {
         if (p) cudaFree(p);
     for (int t = 0; t < N_TYPES; ++t) c->rows[t].release();
     DBuf* bufs[] = {&c->rows_tmp, &c->sort_keys, &c->sort_keys_alt, &c->sort_vals, &c->sort_vals_alt, &c->flags, &c->scan,
-                    &c->cub_tmp, &c->big_flags, &c->big_list, &c->c_g, &c->c_H, &c->c_keys, &c->c_keys_alt, &c->c_vals, &c->c_vals_alt, &c->c_ukeys,
+                    &c->cub_tmp, &c->big_flags, &c->big_list, &c->ccd_work, &c->c_g, &c->c_H, &c->c_keys, &c->c_keys_alt, &c->c_vals, &c->c_vals_alt, &c->c_ukeys,
                     &c->c_ucount, &c->c_ustart, &c->c_val, &c->c_rowptr, &c->c_col, &c->pcg_vec, &c->pcg_part, &c->scal, &c->red, &c->mlp_dist};
     for (DBuf* b : bufs) b->release();
     Grid* gs[] = {&c->gp, &c->ge};

@@ -320,32 +320,48 @@ FIPC_HD bool edge_edge_ctcd(v3 q0s, v3 p0s, v3 q1s, v3 p1s, v3 q0e, v3 p0e, v3 q
     return col;
 }
 
+// The additive lower bound of wrapper.cpp:254-328: lb = (1 - eta) sqrt(dist2) / maxDisp is the
+// time before which the distance cannot drop below eta sqrt(dist2).  False when the pair's toc is
+// 1 without the exact test (no motion, or lb >= 1); else *lb holds the bound.
+FIPC_HD bool pt_needs_exact(v3 dp, v3 dt0, v3 dt1, v3 dt2, double eta, double dist2, double* lb) {
+    const double maxDisp = sqrt(sq(dp)) + sqrt(fmax(fmax(sq(dt0), sq(dt1)), sq(dt2)));
+    if (maxDisp == 0) return false;
+    *lb = (1 - eta) * sqrt(dist2) / maxDisp;
+    return *lb < 1;
+}
+FIPC_HD bool ee_needs_exact(v3 da0, v3 da1, v3 db0, v3 db1, double eta, double dist2, double* lb) {
+    const double maxDisp = sqrt(fmax(sq(da0), sq(da1))) + sqrt(fmax(sq(db0), sq(db1)));
+    if (maxDisp == 0) return false;
+    *lb = (1 - eta) * sqrt(dist2) / maxDisp;
+    return *lb < 1;
+}
+
+// the exact interval test, its toc clamped from below by lb (1 when no collision)
+FIPC_HD double pt_ccd_exact(v3 p, v3 t0, v3 t1, v3 t2, v3 dp, v3 dt0, v3 dt1, v3 dt2, double eta, double dist2, double lb) {
+    double toc = 1.0;
+    if (vertex_face_ctcd(p, t0, t1, t2, p + dp, t0 + dt0, t1 + dt1, t2 + dt2, eta * sqrt(dist2), &toc))
+        if (toc < lb) toc = lb;
+    return toc;
+}
+FIPC_HD double ee_ccd_exact(v3 a0, v3 a1, v3 b0, v3 b1, v3 da0, v3 da1, v3 db0, v3 db1, double eta, double dist2, double lb) {
+    double toc = 1.0;
+    if (edge_edge_ctcd(a0, a1, b0, b1, a0 + da0, a1 + da1, b0 + db0, b1 + db1, eta * sqrt(dist2), &toc))
+        if (toc < lb) toc = lb;
+    return toc;
+}
+
 // additive lower bound + exact test for a point-triangle pair (wrapper.cpp:254-290)
 FIPC_HD double pt_ccd(v3 p, v3 t0, v3 t1, v3 t2, v3 dp, v3 dt0, v3 dt1, v3 dt2, double eta, double dist2) {
-    double toc = 1.0;
-    const double maxDisp = sqrt(sq(dp)) + sqrt(fmax(fmax(sq(dt0), sq(dt1)), sq(dt2)));
-    if (maxDisp != 0) {
-        const double lb = (1 - eta) * sqrt(dist2) / maxDisp;
-        if (lb < 1) {
-            if (vertex_face_ctcd(p, t0, t1, t2, p + dp, t0 + dt0, t1 + dt1, t2 + dt2, eta * sqrt(dist2), &toc))
-                if (toc < lb) toc = lb;
-        }
-    }
-    return toc;
+    double lb;
+    if (!pt_needs_exact(dp, dt0, dt1, dt2, eta, dist2, &lb)) return 1.0;
+    return pt_ccd_exact(p, t0, t1, t2, dp, dt0, dt1, dt2, eta, dist2, lb);
 }
 
 // additive lower bound + exact test for an edge-edge pair (wrapper.cpp:292-328)
 FIPC_HD double ee_ccd(v3 a0, v3 a1, v3 b0, v3 b1, v3 da0, v3 da1, v3 db0, v3 db1, double eta, double dist2) {
-    double toc = 1.0;
-    const double maxDisp = sqrt(fmax(sq(da0), sq(da1))) + sqrt(fmax(sq(db0), sq(db1)));
-    if (maxDisp != 0) {
-        const double lb = (1 - eta) * sqrt(dist2) / maxDisp;
-        if (lb < 1) {
-            if (edge_edge_ctcd(a0, a1, b0, b1, a0 + da0, a1 + da1, b0 + db0, b1 + db1, eta * sqrt(dist2), &toc))
-                if (toc < lb) toc = lb;
-        }
-    }
-    return toc;
+    double lb;
+    if (!ee_needs_exact(da0, da1, db0, db1, eta, dist2, &lb)) return 1.0;
+    return ee_ccd_exact(a0, a1, b0, b1, da0, da1, db0, db1, eta, dist2, lb);
 }
 
 // ---------------------------------------------------------------- inversion-free step
@@ -413,16 +429,39 @@ FIPC_HD double cubic_root_pos(double a, double b, double c, double d, double tol
     return t;
 }
 
-// largest step keeping the tet's orientation, scaled by (1 - eta); 1 if none (math_tools.py:161-181)
-FIPC_HD double inversion_free_step(const v3* X, const v3* P, double eta) {
+// coefficients of det(Ds + t dDs) = a t^3 + b t^2 + c t + d (6 x the tet's volume along the step)
+FIPC_HD void inversion_cubic(const v3* X, const v3* P, double* k) {
     const v3 v01 = X[1] - X[0], v02 = X[2] - X[0], v03 = X[3] - X[0];
     const v3 p01 = P[1] - P[0], p02 = P[2] - P[0], p03 = P[3] - P[0];
     const v3 pp = cross(p01, p02);
     const v3 mix = cross(v01, p02) + cross(p01, v02);
     const v3 vv = cross(v01, v02);
-    const double a = dot(p03, pp), b = dot(v03, pp) + dot(p03, mix), c = dot(p03, vv) + dot(v03, mix), d = dot(v03, vv);
-    const double r = cubic_root_pos(a, b, c, d, 1e-8);
+    k[0] = dot(p03, pp);
+    k[1] = dot(v03, pp) + dot(p03, mix);
+    k[2] = dot(p03, vv) + dot(v03, mix);
+    k[3] = dot(v03, vv);
+}
+
+// largest step keeping the tet's orientation, scaled by (1 - eta); 1 if none (math_tools.py:161-181)
+FIPC_HD double inversion_free_step(const v3* X, const v3* P, double eta) {
+    double k[4];
+    inversion_cubic(X, P, k);
+    const double r = cubic_root_pos(k[0], k[1], k[2], k[3], 1e-8);
     return r < 0.0 ? 1.0 : r * (1.0 - eta);
+}
+
+// Early-out of the step filter for tets whose result is provably >= 1, a no-op in the minimum
+// over all of them (the filter's minimum starts at 1).
+// A tet whose volume polynomial stays above d / 2 on [0, T], T = 2 / (1 - eta), because
+// |c| T + |b| T^2 + |a| T^3 <= d / 2, has no root below T: inversion_free_step returns 1 (no
+// positive root) or (1 - eta) r >= 2.
+FIPC_HD bool inversion_cannot_flip(const v3* X, const v3* P, double eta) {
+    if (!(eta < 1.0)) return false;
+    double k[4];
+    inversion_cubic(X, P, k);
+    if (!(k[3] > 0.0)) return false;
+    const double T = 2.0 / (1.0 - eta);
+    return ((fabs(k[0]) * T + fabs(k[1])) * T + fabs(k[2])) * T <= 0.5 * k[3];
 }
 
 }  // namespace fipc

@@ -11,8 +11,8 @@
 // Aggregates are runs of cs_agg_rows vertices, a multiple of the PCG block, so each PCG block
 // restricts its residuals into its own aggregate with one fixed-order block sum, and the
 // aggregate's last block (atomic ticket) totals them.  Ac is built from the elastic + inertia
-// blocks (one CTA per coupled aggregate pair, fixed-order sums), inverted densely in place by
-// blocked Gauss-Jordan in one cooperative launch, and applied per PCG iteration as one dense
+// blocks (one CTA per coupled aggregate pair, fixed-order sums), inverted densely in place by a
+// symmetric block sweep in one cooperative launch, and applied per PCG iteration as one dense
 // matrix-vector kernel followed by the prolongation.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
@@ -134,91 +134,167 @@ __global__ void k_cs_regularize(int n, double* __restrict__ Ac) {
     *dk = *dk > 0.0 ? *dk * (1.0 + 1e-12) : 1.0;
 }
 
-// In-place blocked Gauss-Jordan inverse of the SPD matrix A (n x n, n a multiple of GJ_B; no
-// pivoting is needed: every diagonal block met is a diagonal block of a Schur complement of an
-// SPD matrix).  One cooperative launch; per block column K three phases separated by grid
-// barriers:
-//   1. T = A_KK^-1 (one CTA, Gauss-Jordan in shared memory); every CTA copies column panel C = A_*K
-//   2. R = T A_K*                                   (row panel)
-//   3. A_KK = T, A_KJ = R_J, A_IK = -C_I T, A_IJ -= C_I R_J   (32 x 32 tiles in shared memory)
-// buf: T (B^2) + C (n B) + R (B n) doubles.
+// In-place inverse of the SPD matrix A (n x n row-major, n a multiple of GJ_B) by the symmetric
+// block sweep (the Gauss-Jordan sweep operator): sweeping block K of a symmetric matrix maps
+//     A_KK -> -A_KK^-1,  A_IK -> A_IK T,  A_KJ -> T A_KJ,  A_IJ -> A_IJ - A_IK T A_KJ   (T = A_KK^-1),
+// which keeps the matrix symmetric, and sweeping every block leaves -A^-1.  No pivoting is
+// needed: the A_KK met are Schur complements of an SPD matrix.  Only the tiles on and below the
+// diagonal are kept, which halves the FP64 work of a full Gauss-Jordan inverse; the upper
+// triangle is filled at the end.  One cooperative launch:
+//   prologue   CTA 0: T = A_00^-1 (Gauss-Jordan on one tile in shared memory)
+//   per K      A: every CTA: panel P_I = A_IK (tile (K, I) transposed for I < K) and W_I = P_I T
+//              B: CTA 0 writes A_KK = -T, then updates tile (K+1, K+1) and inverts it into T
+//                 (the next block's T, ready by the next barrier); the other CTAs take the other
+//                 lower tiles: A_IJ -= W_I P_J^T, A_IK = W_I, A_KJ = W_J^T
+//   epilogue   upper triangle = -(lower triangle)^T, then the lower triangle negated
+// buf: T (B^2) + P (n B) + W (n B) doubles.  Every sum runs in a fixed order.
 constexpr int GJ_B = 32, GJ_THREADS = 256;
+
+// in-place Gauss-Jordan inverse of the SPD tile s (shared memory, row stride GJ_B + 1)
+__device__ void gj_tile_inverse(double (*s)[GJ_B + 1], double* prow, double* pcol) {
+    const int t = threadIdx.x;
+    for (int k = 0; k < GJ_B; ++k) {
+        if (t < GJ_B) {
+            const double inv = 1.0 / s[k][k];
+            prow[t] = t == k ? inv : s[k][t] * inv;
+            pcol[t] = s[t][k];
+        }
+        __syncthreads();
+        for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
+            const int i = e / GJ_B, j = e % GJ_B;
+            double v;
+            if (i == k) v = prow[j];
+            else if (j == k) v = -pcol[i] * prow[k];
+            else v = fma(-pcol[i], prow[j], s[i][j]);
+            s[i][j] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// lower tile number t -> (I, J), I >= J
+__device__ __forceinline__ void lower_tile(int t, int& I, int& J) {
+    int i = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+    while ((i + 1) * (i + 2) / 2 <= t) ++i;
+    while (i * (i + 1) / 2 > t) --i;
+    I = i;
+    J = t - i * (i + 1) / 2;
+}
+
 __global__ void __launch_bounds__(GJ_THREADS) k_cs_gauss_jordan(int n, double* __restrict__ A, double* __restrict__ buf) {
     cg::grid_group grid = cg::this_grid();
     __shared__ double sa[GJ_B][GJ_B + 1];
     __shared__ double sb[GJ_B][GJ_B + 1];
-    __shared__ double piv[GJ_B], pcol[GJ_B];
+    __shared__ double prow[GJ_B], pcol[GJ_B];
     const int nb = n / GJ_B, t = threadIdx.x;
     const long long gtid = (long long)blockIdx.x * GJ_THREADS + t, gthr = (long long)gridDim.x * GJ_THREADS;
     double* T = buf;
-    double* C = buf + GJ_B * GJ_B;
-    double* R = C + (size_t)n * GJ_B;
+    double* P = buf + GJ_B * GJ_B;
+    double* W = P + (size_t)n * GJ_B;
+    const int c = t & 31, rb = t >> 5;   // tile column and first row (rows rb, rb + 8, rb + 16, rb + 24)
+    const bool solo = gridDim.x == 1;
+    const int worker = solo ? 0 : (int)blockIdx.x - 1, workers = solo ? 1 : (int)gridDim.x - 1;
+    const int n_lower = nb * (nb + 1) / 2;
+    if (blockIdx.x == 0) {
+        for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) sa[e / GJ_B][e % GJ_B] = A[(size_t)(e / GJ_B) * n + e % GJ_B];
+        __syncthreads();
+        gj_tile_inverse(sa, prow, pcol);
+        for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) T[e] = sa[e / GJ_B][e % GJ_B];
+    }
+    grid.sync();
     for (int K = 0; K < nb; ++K) {
         const int k0 = K * GJ_B;
-        // phase 1
-        if (blockIdx.x == 0) {
-            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) sa[e / GJ_B][e % GJ_B] = A[(size_t)(k0 + e / GJ_B) * n + k0 + e % GJ_B];
-            __syncthreads();
-            for (int k = 0; k < GJ_B; ++k) {
-                if (t < GJ_B) {
-                    piv[t] = sa[k][t];
-                    pcol[t] = sa[t][k];
-                }
-                __syncthreads();
-                const double inv = 1.0 / piv[k];
-                for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
-                    const int i = e / GJ_B, j = e % GJ_B;
-                    double v;
-                    if (i == k) v = (j == k) ? inv : piv[j] * inv;
-                    else if (j == k) v = -pcol[i] * inv;
-                    else v = sa[i][j] - pcol[i] * piv[j] * inv;
-                    sa[i][j] = v;
-                }
-                __syncthreads();
-            }
-            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) T[e] = sa[e / GJ_B][e % GJ_B];
-        }
-        for (long long e = gtid; e < (long long)n * GJ_B; e += gthr) {
-            const int i = (int)(e / GJ_B), m = (int)(e % GJ_B);
-            C[e] = A[(size_t)i * n + k0 + m];
-        }
-        grid.sync();
-        // phase 2: R[k][j] = sum_m T[k][m] A[k0 + m][j]
-        for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) sb[e / GJ_B][e % GJ_B] = T[e];
+        // A: P_I and W_I = P_I T for every row outside block K
+        for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) sa[e / GJ_B][e % GJ_B] = T[e];
         __syncthreads();
         for (long long e = gtid; e < (long long)n * GJ_B; e += gthr) {
-            const int k = (int)(e / n), j = (int)(e % n);
-            double v = 0.0;
+            const int i = (int)(e / GJ_B), m = (int)(e % GJ_B), I = i / GJ_B;
+            if (I == K) continue;
+            const double* src = I > K ? A + (size_t)i * n + k0 : A + (size_t)k0 * n + i;
+            const size_t st = I > K ? 1 : (size_t)n;
+            double w = 0.0;
 #pragma unroll 8
-            for (int m = 0; m < GJ_B; ++m) v += sb[k][m] * A[(size_t)(k0 + m) * n + j];
-            R[(size_t)k * n + j] = v;
+            for (int q = 0; q < GJ_B; ++q) w = fma(src[q * st], sa[q][m], w);
+            P[e] = src[m * st];
+            W[e] = w;
         }
         grid.sync();
-        // phase 3, one 32 x 32 tile per CTA iteration
-        for (int tile = blockIdx.x; tile < nb * nb; tile += gridDim.x) {
-            const int I = tile / nb, J = tile % nb, i0 = I * GJ_B, j0 = J * GJ_B;
-            __syncthreads();
-            // sa = C_I (rows i0.., 32 columns); sb = R_J or T
-            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
-                const int r = e / GJ_B, c = e % GJ_B;
-                sa[r][c] = C[(size_t)(i0 + r) * GJ_B + c];
-                sb[r][c] = (J == K) ? T[r * GJ_B + c] : R[(size_t)r * n + j0 + c];
+        // B
+        if (blockIdx.x == 0) {
+            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) A[(size_t)(k0 + e / GJ_B) * n + k0 + e % GJ_B] = -T[e];
+            if (K + 1 < nb) {
+                const int i0 = k0 + GJ_B;
+                __syncthreads();
+                for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
+                    sa[e / GJ_B][e % GJ_B] = W[(size_t)i0 * GJ_B + e];
+                    sb[e / GJ_B][e % GJ_B] = P[(size_t)i0 * GJ_B + e];
+                }
+                __syncthreads();
+                double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int q = 0; q < GJ_B; ++q) {
+                    const double pj = sb[c][q];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) acc[u] = fma(sa[rb + 8 * u][q], pj, acc[u]);
+                }
+                double v[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) v[u] = A[(size_t)(i0 + rb + 8 * u) * n + i0 + c] - acc[u];
+                __syncthreads();
+#pragma unroll
+                for (int u = 0; u < 4; ++u) sa[rb + 8 * u][c] = v[u];
+                __syncthreads();
+                gj_tile_inverse(sa, prow, pcol);
+                for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) T[e] = sa[e / GJ_B][e % GJ_B];
             }
-            __syncthreads();
-            for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
-                const int r = e / GJ_B, c = e % GJ_B;
-                double* out = A + (size_t)(i0 + r) * n + j0 + c;
-                if (I == K) {
-                    *out = sb[r][c];            // T on the diagonal tile, R_J elsewhere
-                } else {
-                    double v = 0.0;
-#pragma unroll 8
-                    for (int m = 0; m < GJ_B; ++m) v += sa[r][m] * sb[m][c];
-                    *out = (J == K) ? -v : *out - v;
+        }
+        if (blockIdx.x != 0 || solo) {
+            for (int tile = worker; tile < n_lower; tile += workers) {
+                int I, J;
+                lower_tile(tile, I, J);
+                if ((I == K && J == K) || (I == K + 1 && J == K + 1)) continue;
+                const int i0 = I * GJ_B, j0 = J * GJ_B;
+                if (J == K) {            // A_IK = W_I (I > K)
+                    for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS)
+                        A[(size_t)(i0 + e / GJ_B) * n + k0 + e % GJ_B] = W[(size_t)i0 * GJ_B + e];
+                    continue;
+                }
+                if (I == K) {            // A_KJ = W_J^T (J < K)
+                    for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
+                        const int r = e / GJ_B, cc = e % GJ_B;
+                        A[(size_t)(k0 + r) * n + j0 + cc] = W[(size_t)(j0 + cc) * GJ_B + r];
+                    }
+                    continue;
+                }
+                __syncthreads();
+                for (int e = t; e < GJ_B * GJ_B; e += GJ_THREADS) {
+                    sa[e / GJ_B][e % GJ_B] = W[(size_t)i0 * GJ_B + e];
+                    sb[e / GJ_B][e % GJ_B] = P[(size_t)j0 * GJ_B + e];
+                }
+                __syncthreads();
+                double acc[4] = {0.0, 0.0, 0.0, 0.0};
+                for (int q = 0; q < GJ_B; ++q) {
+                    const double pj = sb[c][q];
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) acc[u] = fma(sa[rb + 8 * u][q], pj, acc[u]);
+                }
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    double* out = A + (size_t)(i0 + rb + 8 * u) * n + j0 + c;
+                    *out = *out - acc[u];
                 }
             }
         }
         grid.sync();
+    }
+    // epilogue: the lower triangle holds -A^-1
+    for (long long e = gtid; e < (long long)n * n; e += gthr) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        if (i < j) A[e] = -A[(size_t)j * n + i];
+    }
+    grid.sync();
+    for (long long e = gtid; e < (long long)n * n; e += gthr) {
+        const int i = (int)(e / n), j = (int)(e % n);
+        if (i >= j) A[e] = -A[e];
     }
 }
 
@@ -230,7 +306,7 @@ static int launch_gauss_jordan(int n, double* A, double* buf, cudaStream_t s) {
     FIPC_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_cs_gauss_jordan, GJ_THREADS, 0));
     if (per < 1) return FIPC_ERR_CUDA;
     int grid = nsm * (per < 2 ? per : 2);
-    const int tiles = (n / GJ_B) * (n / GJ_B);
+    const int nb = n / GJ_B, tiles = nb * (nb + 1) / 2 + 1;   // the lower tiles, plus CTA 0's own work
     if (grid > tiles) grid = tiles;
     void* args[] = {&n, &A, &buf};
     FIPC_CUDA(cudaLaunchCooperativeKernel((const void*)k_cs_gauss_jordan, dim3(grid), dim3(GJ_THREADS), args, 0, s));
@@ -313,7 +389,7 @@ int cs_setup(fipc_ctx* c, int agg_rows, const int* row_ptr_h, const int* col_idx
 
 int mg_offsets(fipc_ctx* c, const double* x, cudaStream_t s);
 
-// the blocked Gauss-Jordan inverse for other preconditioner levels (n a multiple of GJ_B)
+// the symmetric block-sweep inverse for other preconditioner levels (n a multiple of GJ_B)
 int cs_gauss_jordan(int n, double* A, double* buf, cudaStream_t s) { return launch_gauss_jordan(n, A, buf, s); }
 
 // offsets from the aggregate centroids at the Newton iterate x (called by the assembly), and the

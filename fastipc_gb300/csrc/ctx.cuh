@@ -117,6 +117,7 @@ struct fipc_ctx_impl {
     // [2] (device, 3 x (n_scenes + 1)); big-primitive flags and lists of the spatial hash
     int* prim_off = nullptr;
     DBuf big_flags, big_list;
+    DBuf ccd_work;                        // step filter: pairs left to the exact test, and their counts
     std::vector<double> h_kappa, h_inv_dx;
     // batched PCG: tiles of consecutive rows inside one scene
     int n_tiles = 0, tile_rows = 0, pcg_grid = 0;
@@ -132,6 +133,7 @@ struct fipc_ctx_impl {
     // above); an MgState owned by the context
     void* mg = nullptr;
     int mg_levels = 0;
+    int mg_fp32 = 1;                      // FP32 level-0 smoothing products in the V-cycle (the default)
     // the last direct solve: fronts, their storage (doubles), factorisation flops, host analysis time
     int mf_fronts = 0;
     long long mf_front_doubles = 0;

@@ -4,7 +4,7 @@
 //     level 0 (vertices, 3x3 blocks):  z = w0 D^-1 r;  t = r - A z;  restrict;  ...;  prolong;
 //                                      u = z + w0 D^-1 (r - A z)            (u: the PCG's B r)
 //     levels 1 .. L-2 (6x6 blocks):    the same on the Galerkin matrices A_l = P^T A_{l-1} P
-//     level L-1 (coarsest):            dense inverse (blocked Gauss-Jordan)
+//     level L-1 (coarsest):            dense inverse (symmetric block sweep)
 //
 // D^-1 is the block-Jacobi inverse (level 0: the PCG's own, identity at Dirichlet vertices) and
 // w_l = 4 / (3 * 1.05 * rho_l) with rho_l an 8-step power-iteration estimate of the spectral
@@ -30,7 +30,7 @@
 namespace fipc {
 
 int cs_gauss_jordan(int n, double* A, double* buf, cudaStream_t s);
-constexpr int MG_GJ_B = 32;                 // block of the Gauss-Jordan inverse (its row padding)
+constexpr int MG_GJ_B = 32;                 // block of the dense inverse (its row padding)
 constexpr int MG_POWER_ITERS = 8;          // power iterations per level and solve
 constexpr int MG_THREADS = 128;
 constexpr int MG_MIN_VERTICES = 1000;      // smaller scenes keep the two-level preconditioner
@@ -43,13 +43,13 @@ int mg_offsets(fipc_ctx* c, const double* x, cudaStream_t s);
 
 // device buffers of one level
 struct MgLevelBufs {
-    DBuf mem_ptr, mem, agg_of;                       // levels >= 1
+    DBuf mem_ptr, mem, agg_of, rot;                  // levels >= 1 (rot: level 1)
     DBuf s_rp, s_ci, s_cp, s_src, s_row, s_col;      // static pattern and contributions
     DBuf c_rp, c_ci, c_cp, c_src, c_row, c_col;      // contact pattern and contributions
     DBuf s_val, c_val, minv, cent, d, g, z, z2, t;   // values, inverses, geometry, vectors
     DBuf pv0, pv1, part, nrm;                        // power iteration
     void release() {
-        DBuf* all[] = {&mem_ptr, &mem, &agg_of, &s_rp, &s_ci, &s_cp, &s_src, &s_row, &s_col, &c_rp, &c_ci, &c_cp, &c_src, &c_row,
+        DBuf* all[] = {&mem_ptr, &mem, &agg_of, &rot, &s_rp, &s_ci, &s_cp, &s_src, &s_row, &s_col, &c_rp, &c_ci, &c_cp, &c_src, &c_row,
                        &c_col, &s_val, &c_val, &minv, &cent, &d, &g, &z, &z2, &t, &pv0, &pv1, &part, &nrm};
         for (DBuf* b : all) b->release();
     }
@@ -58,13 +58,14 @@ struct MgLevelBufs {
 struct MgState {
     MgPlan plan;
     std::vector<MgLevelBufs> B;
-    DBuf dense, gj_buf, omega, t0, z0, terms;
+    DBuf dense, gj_buf, omega, t0, z0, terms, v32, z0f;
     int n_dense = 0, ld_dense = 0;
+    bool fp32 = false;                               // FP32 smoothing products on level 0
     bool contact_empty = true;                       // the per-level contact patterns are empty
     MgArgs args{};                                   // kernel arguments of the V-cycle
     ~MgState() {
         for (MgLevelBufs& b : B) b.release();
-        DBuf* all[] = {&dense, &gj_buf, &omega, &t0, &z0, &terms};
+        DBuf* all[] = {&dense, &gj_buf, &omega, &t0, &z0, &terms, &v32, &z0f};
         for (DBuf* b : all) b->release();
     }
 };
@@ -80,7 +81,7 @@ static int upload_vec(DBuf& b, const std::vector<T>& v, cudaStream_t s) {
 // centroid of each aggregate of level l from its members' positions (vertices: x; nodes: the
 // finer level's centroids), then each member's offset from it
 __global__ void k_mg_centroid(int n, const int* __restrict__ mem_ptr, const int* __restrict__ mem, const double* __restrict__ pos,
-                              double* __restrict__ cent, double* __restrict__ d) {
+                              const unsigned char* __restrict__ rot, double* __restrict__ cent, double* __restrict__ d) {
     const int I = blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= n) return;
     double c0 = 0.0, c1 = 0.0, c2 = 0.0;
@@ -98,11 +99,12 @@ __global__ void k_mg_centroid(int n, const int* __restrict__ mem_ptr, const int*
     cent[3 * (size_t)I] = c0;
     cent[3 * (size_t)I + 1] = c1;
     cent[3 * (size_t)I + 2] = c2;
+    const bool r = !rot || rot[I];   // translation-only nodes: zero offsets, so zero rotation columns
     for (int k = k0; k < k1; ++k) {
         const int i = mem[k];
-        d[3 * (size_t)i] = pos[3 * (size_t)i] - c0;
-        d[3 * (size_t)i + 1] = pos[3 * (size_t)i + 1] - c1;
-        d[3 * (size_t)i + 2] = pos[3 * (size_t)i + 2] - c2;
+        d[3 * (size_t)i] = r ? pos[3 * (size_t)i] - c0 : 0.0;
+        d[3 * (size_t)i + 1] = r ? pos[3 * (size_t)i + 1] - c1 : 0.0;
+        d[3 * (size_t)i + 2] = r ? pos[3 * (size_t)i + 2] - c2 : 0.0;
     }
 }
 
@@ -415,8 +417,19 @@ __global__ void k_mg_scale0(PCGArgs a, double* __restrict__ z0, const double* __
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.nV) return;
     const double w = omega[0];
-    for (int k = 0; k < 3; ++k) z0[4 * (size_t)i + k] = w * a.u[4 * (size_t)i + k];
+    for (int k = 0; k < 3; ++k) {
+        const double v = w * a.u[4 * (size_t)i + k];
+        z0[4 * (size_t)i + k] = v;
+        if (a.mg_z0f) a.mg_z0f[4 * (size_t)i + k] = (float)v;
+    }
     z0[4 * (size_t)i + 3] = 0.0;
+    if (a.mg_z0f) a.mg_z0f[4 * (size_t)i + 3] = 0.f;
+}
+
+// FP32 copies of the level-0 values (elastic sliced ELL, contact blocks) for the smoothing products
+__global__ void k_mg_to_f32(long long n, const double* __restrict__ in, float* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
 }
 
 // t0 = r - A z0 (free vertices; Dirichlet vertices 0)
@@ -430,6 +443,20 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_res0(PCGArgs a, const double
     t0[3 * (size_t)i] = fx ? 0.0 : a.r[3 * (size_t)i] - y0;
     t0[3 * (size_t)i + 1] = fx ? 0.0 : a.r[3 * (size_t)i + 1] - y1;
     t0[3 * (size_t)i + 2] = fx ? 0.0 : a.r[3 * (size_t)i + 2] - y2;
+}
+
+// t0 = r - A z0 with FP32 products (values and z0 as FP32, FP32 sums); the residual in FP64
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_res0_f32(PCGArgs a, const float* __restrict__ v32, const float* __restrict__ c32,
+                                                             const float4* __restrict__ z0f, double* __restrict__ t0) {
+    if (*(volatile int*)&a.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nV) return;
+    float y0 = 0.f, y1 = 0.f, y2 = 0.f;
+    const bool fx = a.fixed[i];
+    if (!fx) row_apply_f32(a, v32, c32, i, z0f, y0, y1, y2);
+    t0[3 * (size_t)i] = fx ? 0.0 : a.r[3 * (size_t)i] - (double)y0;
+    t0[3 * (size_t)i + 1] = fx ? 0.0 : a.r[3 * (size_t)i + 1] - (double)y1;
+    t0[3 * (size_t)i + 2] = fx ? 0.0 : a.r[3 * (size_t)i + 2] - (double)y2;
 }
 
 // restriction of the finer residual t (vertices: stride 3, Dirichlet vertices skipped; nodes:
@@ -518,9 +545,15 @@ __global__ void __launch_bounds__(MG_THREADS) k_mg_prolong(PCGArgs a, MgLev L, c
     const double d0 = L.d[3 * (size_t)i], d1 = L.d[3 * (size_t)i + 1], d2 = L.d[3 * (size_t)i + 2];
     const double u0 = Y[0] + (Y[4] * d2 - Y[5] * d1), u1 = Y[1] + (Y[5] * d0 - Y[3] * d2), u2 = Y[2] + (Y[3] * d1 - Y[4] * d0);
     if (to_vertices) {
-        zf[4 * (size_t)i] += u0;
-        zf[4 * (size_t)i + 1] += u1;
-        zf[4 * (size_t)i + 2] += u2;
+        const double z0 = zf[4 * (size_t)i] + u0, z1 = zf[4 * (size_t)i + 1] + u1, z2 = zf[4 * (size_t)i + 2] + u2;
+        zf[4 * (size_t)i] = z0;
+        zf[4 * (size_t)i + 1] = z1;
+        zf[4 * (size_t)i + 2] = z2;
+        if (a.mg_z0f) {
+            a.mg_z0f[4 * (size_t)i] = (float)z0;
+            a.mg_z0f[4 * (size_t)i + 1] = (float)z1;
+            a.mg_z0f[4 * (size_t)i + 2] = (float)z2;
+        }
     } else {
         double* z = zf + 6 * (size_t)i;
         z[0] += u0;
@@ -544,6 +577,27 @@ __global__ void __launch_bounds__(PCG_THREADS) k_mg_post0(PCGArgs a, const doubl
     double y0, y1, y2;
     row_apply<4>(a, i, z0, y0, y1, y2);
     const double s0 = a.r[3 * (size_t)i] - y0, s1 = a.r[3 * (size_t)i + 1] - y1, s2 = a.r[3 * (size_t)i + 2] - y2;
+    const double* M = a.minv + 9 * (size_t)i;
+    const double w = omega[0];
+    a.u[4 * (size_t)i] = z0[4 * (size_t)i] + w * (M[0] * s0 + M[1] * s1 + M[2] * s2);
+    a.u[4 * (size_t)i + 1] = z0[4 * (size_t)i + 1] + w * (M[3] * s0 + M[4] * s1 + M[5] * s2);
+    a.u[4 * (size_t)i + 2] = z0[4 * (size_t)i + 2] + w * (M[6] * s0 + M[7] * s1 + M[8] * s2);
+}
+
+// the same with FP32 products
+__global__ void __launch_bounds__(PCG_THREADS) k_mg_post0_f32(PCGArgs a, const float* __restrict__ v32, const float* __restrict__ c32,
+                                                              const float4* __restrict__ z0f, const double* __restrict__ z0,
+                                                              const double* __restrict__ omega) {
+    if (*(volatile int*)&a.flag[0]) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nV) return;
+    if (a.fixed[i]) {
+        a.u[4 * (size_t)i] = a.u[4 * (size_t)i + 1] = a.u[4 * (size_t)i + 2] = 0.0;
+        return;
+    }
+    float y0, y1, y2;
+    row_apply_f32(a, v32, c32, i, z0f, y0, y1, y2);
+    const double s0 = a.r[3 * (size_t)i] - (double)y0, s1 = a.r[3 * (size_t)i + 1] - (double)y1, s2 = a.r[3 * (size_t)i + 2] - (double)y2;
     const double* M = a.minv + 9 * (size_t)i;
     const double w = omega[0];
     a.u[4 * (size_t)i] = z0[4 * (size_t)i] + w * (M[0] * s0 + M[1] * s1 + M[2] * s2);
@@ -589,6 +643,7 @@ int mg_setup(fipc_ctx* c, double h) {
         st |= upload_vec(b.mem_ptr, p.mem_ptr, s);
         st |= upload_vec(b.mem, p.mem, s);
         st |= upload_vec(b.agg_of, p.agg_of, s);
+        if (l == 1) st |= upload_vec(b.rot, p.rot, s);
         st |= upload_vec(b.s_rp, p.S.rp, s);
         st |= upload_vec(b.s_ci, p.S.ci, s);
         st |= upload_vec(b.s_cp, p.S.con_ptr, s);
@@ -642,6 +697,7 @@ int mg_offsets(fipc_ctx* c, const double* x, cudaStream_t s) {
         const int n = M->plan.L[l].n;
         const double* pos = l == 1 ? x : M->B[l - 1].cent.as<double>();
         k_mg_centroid<<<nblk_m(n, MG_THREADS), MG_THREADS, 0, s>>>(n, M->B[l].mem_ptr.as<int>(), M->B[l].mem.as<int>(), pos,
+                                                                    l == 1 ? M->B[l].rot.as<unsigned char>() : nullptr,
                                                                     M->B[l].cent.as<double>(), M->B[l].d.as<double>());
         FIPC_LAUNCHED();
     }
@@ -656,6 +712,7 @@ int mg_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
     a.mg = nullptr;
     a.mg_z0 = nullptr;
     a.mg_omega = nullptr;
+    a.mg_z0f = nullptr;
     if (!M) return FIPC_OK;
     const int NL = M->plan.levels, nV = c->nV;
     // contact patterns of every level
@@ -770,9 +827,25 @@ int mg_prepare(fipc_ctx* c, const unsigned char* fixed, PCGArgs& a, cudaStream_t
         L.z2 = b.z2.as<double>();
         L.t = b.t.as<double>();
     }
+    M->fp32 = c->mg_fp32 != 0;
+    if (M->fp32) {
+        const long long ne = 288ll * c->n_slots, nc = 9ll * c->c_nnzb;
+        if (M->v32.ensure(4ull * (ne + nc) + 64) || M->z0f.ensure(16ull * nV + 64)) return FIPC_ERR_CUDA;
+        float* v32 = M->v32.as<float>();
+        k_mg_to_f32<<<1216, 256, 0, s>>>(ne, c->sell_val, v32);
+        FIPC_LAUNCHED();
+        if (nc) {
+            k_mg_to_f32<<<nblk_m(nc, 256), 256, 0, s>>>(nc, c->c_val.as<double>(), v32 + ne);
+            FIPC_LAUNCHED();
+        }
+        m.v32 = v32;
+        m.c32 = v32 + ne;
+        m.z0f = M->z0f.as<float>();
+    }
     a.mg = &M->args;
     a.mg_z0 = m.z0;
     a.mg_omega = m.omega;
+    a.mg_z0f = m.z0f;
     FIPC_CUDA(cudaGetLastError());
     return FIPC_OK;
 }
@@ -819,7 +892,8 @@ void mg_vcycle(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s) {
     const MgArgs& m = M->args;
     const int NL = m.levels, nV = c->nV;
     const int nb0 = nblk_m(nV, PCG_THREADS);
-    k_mg_res0<<<nb0, PCG_THREADS, 0, s>>>(a, m.z0, m.t0);
+    if (m.z0f) k_mg_res0_f32<<<nb0, PCG_THREADS, 0, s>>>(a, m.v32, m.c32, reinterpret_cast<const float4*>(m.z0f), m.t0);
+    else k_mg_res0<<<nb0, PCG_THREADS, 0, s>>>(a, m.z0, m.t0);
     for (int l = 1; l < NL; ++l) {
         const MgLev& L = m.L[l];
         k_mg_restrict<<<nblk_m(32ll * L.n, MG_THREADS), MG_THREADS, 0, s>>>(a, L, l == 1 ? m.t0 : m.L[l - 1].t, l == 1, m.omega + l,
@@ -834,7 +908,8 @@ void mg_vcycle(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s) {
                                                                     l == 1);
         if (l - 1 >= 1) k_mg_smooth<<<nblk_m(32ll * nf, MG_THREADS), MG_THREADS, 0, s>>>(a, m.L[l - 1], m.omega + (l - 1), 1);
     }
-    k_mg_post0<<<nb0, PCG_THREADS, 0, s>>>(a, m.z0, m.omega);
+    if (m.z0f) k_mg_post0_f32<<<nb0, PCG_THREADS, 0, s>>>(a, m.v32, m.c32, reinterpret_cast<const float4*>(m.z0f), m.z0, m.omega);
+    else k_mg_post0<<<nb0, PCG_THREADS, 0, s>>>(a, m.z0, m.omega);
     g_launches.fetch_add(mg_launches_per_cycle(NL), std::memory_order_relaxed);
 }
 
@@ -843,6 +918,14 @@ void mg_vcycle(const fipc_ctx* c, const PCGArgs& a, cudaStream_t s) {
 int mg_launches_per_cycle(int levels) { return 4 * levels - 3; }
 
 }  // namespace fipc
+
+extern "C" int fipc_ctx_set_multigrid_fp32(fipc_ctx* c, int on) {
+    using namespace fipc;
+    if (!c) return FIPC_ERR_ARGUMENT;
+    c->mg_fp32 = on ? 1 : 0;
+    pcg_graph_reset(c);
+    return FIPC_OK;
+}
 
 extern "C" int fipc_ctx_multigrid(fipc_ctx* c, int* levels, int* nodes_h) {
     using namespace fipc;

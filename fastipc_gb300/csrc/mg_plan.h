@@ -40,6 +40,7 @@ struct MgLevelPlan {
     int n = 0;                       // nodes of this level (level 0: vertices)
     std::vector<int> agg_of;         // [n_{l-1}] aggregate of each finer node (levels >= 1)
     std::vector<int> mem_ptr, mem;   // members of each node (finer-level ids, ascending)
+    std::vector<unsigned char> rot;  // level 1: 1 = the node carries rotations, 0 = translations only
     MgPattern S;                     // static pattern (level 0: the system's elastic pattern)
     MgPattern C;                     // contact pattern (rebuilt by mg_contact)
 };
@@ -167,6 +168,36 @@ inline void mg_build(int nV, const double* x0, const int* rp, const int* ci, dou
                 for (int d = 0; d < 3; ++d) cp[3 * a + d] += pos[3 * c.mem[k] + d];
             for (int d = 0; d < 3; ++d) cp[3 * a + d] /= (double)(c.mem_ptr[a + 1] - c.mem_ptr[a]);
             cc[a] = ncomp[c.mem[c.mem_ptr[a]]];
+        }
+        // level 1: an aggregate of vertices on one line (one or two vertices, or collinear ones)
+        // has a rank-deficient rotation block (the rotation about that line moves nothing); it
+        // keeps its translations only, so that its rotation rows of every coarse matrix are
+        // exactly zero instead of rounding noise
+        if (P.L.size() == 1) {
+            c.rot.assign(na, 1);
+            for (int a = 0; a < na; ++a) {
+                double far2 = 0.0, u[3] = {0.0, 0.0, 0.0};
+                for (int k = c.mem_ptr[a]; k < c.mem_ptr[a + 1]; ++k) {
+                    double dv[3], d2 = 0.0;
+                    for (int q = 0; q < 3; ++q) {
+                        dv[q] = pos[3 * c.mem[k] + q] - cp[3 * a + q];
+                        d2 += dv[q] * dv[q];
+                    }
+                    if (d2 > far2) {
+                        far2 = d2;
+                        for (int q = 0; q < 3; ++q) u[q] = dv[q];
+                    }
+                }
+                double perp2 = 0.0;
+                if (far2 > 0.0)
+                    for (int k = c.mem_ptr[a]; k < c.mem_ptr[a + 1]; ++k) {
+                        double dv[3];
+                        for (int q = 0; q < 3; ++q) dv[q] = pos[3 * c.mem[k] + q] - cp[3 * a + q];
+                        const double x = dv[1] * u[2] - dv[2] * u[1], y = dv[2] * u[0] - dv[0] * u[2], z = dv[0] * u[1] - dv[1] * u[0];
+                        perp2 = std::max(perp2, (x * x + y * y + z * z) / far2);   // squared distance from the line
+                    }
+                if (!(perp2 > 1e-12 * far2)) c.rot[a] = 0;
+            }
         }
         pos.swap(cp);
         ncomp.swap(cc);

@@ -32,6 +32,7 @@ struct PCGArgs {
     const struct MgArgs* mg;
     double* mg_z0;
     const double* mg_omega;          // [levels] smoother weights (device)
+    float* mg_z0f;                   // FP32 copy of z0 (stride 4) for FP32 smoothing products, or null
 };
 
 // one level >= 1 of the multigrid hierarchy (6 DOFs per node), as the V-cycle kernels see it
@@ -56,6 +57,10 @@ struct MgArgs {
     const double* omega;             // [levels]
     const double* dense;             // coarsest inverse, row stride ld_dense
     int n_dense, ld_dense;
+    // FP32 smoothing products on level 0 (null: FP64): the elastic values in the sliced-ELL
+    // layout and the contact values as FP32 copies, and z0 as FP32 (stride 4)
+    const float *v32, *c32;
+    float* z0f;
 };
 enum { SC_GAMMA = 0, SC_DELTA, SC_RR, SC_ALPHA, SC_BETA, SC_RR0, SC_TOL2, SC_COUNT };
 constexpr int PCG_THREADS = 128;
@@ -123,6 +128,51 @@ __device__ __forceinline__ void row_apply(const PCGArgs& a, int i, const double*
         y0 = fma(B[0], v0, fma(B[1], v1, fma(B[2], v2, y0)));
         y1 = fma(B[3], v0, fma(B[4], v1, fma(B[5], v2, y1)));
         y2 = fma(B[6], v0, fma(B[7], v1, fma(B[8], v2, y2)));
+    }
+}
+
+// y = A v with FP32 copies of the values (v32: the sliced-ELL layout of sval; c32: the contact
+// blocks) and an FP32 vector (stride 4), accumulated in FP32: the multigrid's smoothing products
+__device__ __forceinline__ void row_apply_f32(const PCGArgs& a, const float* __restrict__ v32, const float* __restrict__ c32, int i,
+                                              const float4* __restrict__ v, float& y0, float& y1, float& y2) {
+    y0 = y1 = y2 = 0.f;
+    const int sl = i >> 5, lane = i & 31;
+    const int base = a.soff[sl], len = a.rlen[i];
+    int k = 0;
+    for (; k + 1 < len; k += 2) {
+        const size_t s0 = (size_t)(base + k), s1 = s0 + 1;
+        const int j0 = __ldg(a.scol + s0 * 32 + lane), j1 = __ldg(a.scol + s1 * 32 + lane);
+        const float* B = v32 + s0 * 288 + lane;
+        const float* C = v32 + s1 * 288 + lane;
+        float b[9], c[9];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) {
+            b[q] = __ldg(B + 32 * q);
+            c[q] = __ldg(C + 32 * q);
+        }
+        const float4 p = __ldg(v + j0), q = __ldg(v + j1);
+        y0 = fmaf(b[0], p.x, fmaf(b[1], p.y, fmaf(b[2], p.z, y0)));
+        y1 = fmaf(b[3], p.x, fmaf(b[4], p.y, fmaf(b[5], p.z, y1)));
+        y2 = fmaf(b[6], p.x, fmaf(b[7], p.y, fmaf(b[8], p.z, y2)));
+        y0 = fmaf(c[0], q.x, fmaf(c[1], q.y, fmaf(c[2], q.z, y0)));
+        y1 = fmaf(c[3], q.x, fmaf(c[4], q.y, fmaf(c[5], q.z, y1)));
+        y2 = fmaf(c[6], q.x, fmaf(c[7], q.y, fmaf(c[8], q.z, y2)));
+    }
+    if (k < len) {
+        const size_t s0 = (size_t)(base + k);
+        const int j0 = __ldg(a.scol + s0 * 32 + lane);
+        const float* B = v32 + s0 * 288 + lane;
+        const float4 p = __ldg(v + j0);
+        y0 = fmaf(__ldg(B + 0), p.x, fmaf(__ldg(B + 32), p.y, fmaf(__ldg(B + 64), p.z, y0)));
+        y1 = fmaf(__ldg(B + 96), p.x, fmaf(__ldg(B + 128), p.y, fmaf(__ldg(B + 160), p.z, y1)));
+        y2 = fmaf(__ldg(B + 192), p.x, fmaf(__ldg(B + 224), p.y, fmaf(__ldg(B + 256), p.z, y2)));
+    }
+    for (int e = a.crp[i]; e < a.crp[i + 1]; ++e) {
+        const float* B = c32 + 9 * (size_t)e;
+        const float4 p = __ldg(v + a.cci[e]);
+        y0 = fmaf(B[0], p.x, fmaf(B[1], p.y, fmaf(B[2], p.z, y0)));
+        y1 = fmaf(B[3], p.x, fmaf(B[4], p.y, fmaf(B[5], p.z, y1)));
+        y2 = fmaf(B[6], p.x, fmaf(B[7], p.y, fmaf(B[8], p.z, y2)));
     }
 }
 

@@ -217,7 +217,7 @@ __device__ __forceinline__ void final_sums(const PCGArgs& a, double (&out)[NV]) 
 }
 
 // residual of the initial guess, block-Jacobi inverse, u = M^-1 r; partials of (r,r)
-__global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const double* __restrict__ rhs, double rtol) {
+__global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const double* __restrict__ rhs, double rtol, int maxit) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     double rr = 0.0, bb = 0.0, r3[3] = {0.0, 0.0, 0.0};
     if (i < a.nV) {
@@ -264,6 +264,7 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_start(PCGArgs a, const doub
         a.flag[1] = 0;
         a.flag[2] = 0;
         a.flag[3] = 0;
+        a.flag[4] = maxit;
     }
 }
 
@@ -349,8 +350,13 @@ __global__ void __launch_bounds__(PCG_THREADS) k_pcg_update(PCGArgs a) {
             a.x[q] = x[d] + alpha * pn[d];
             a.r[q] = rn[d];
             const double z = M[3 * d] * rn[0] + M[3 * d + 1] * rn[1] + M[3 * d + 2] * rn[2];
-            if (a.mg_z0) a.mg_z0[4 * i + d] = a.mg_omega[0] * z;
-            else a.u[4 * i + d] = z;
+            if (a.mg_z0) {
+                const double z0 = a.mg_omega[0] * z;
+                a.mg_z0[4 * i + d] = z0;
+                if (a.mg_z0f) a.mg_z0f[4 * i + d] = (float)z0;
+            } else {
+                a.u[4 * i + d] = z;
+            }
         }
     }
     if (a.cs_blocks) block_restrict(a, i < a.nV, i, rn, d3);
@@ -505,27 +511,39 @@ int sell_to_bsr(fipc_ctx* c, double* out, cudaStream_t s) {
     return FIPC_OK;
 }
 
-// iterations per captured graph of the single-scene PCG: iterations after convergence return at
-// their first instruction, so a chunk overshoots by at most PCG3_CHUNK - 1 empty launches
-constexpr int PCG3_CHUNK = 32;
+// The single-scene PCG replays from one captured graph per solve: a while-loop (conditional)
+// node whose body holds PCG3_BODY iterations (SpMV, update, preconditioner) and a one-thread
+// kernel that keeps the loop going while the solve has not converged and another body fits the
+// iteration budget.  Convergence is decided on the device; the host launches the graph once and
+// reads the flags once.  Iterations after convergence inside the last body return at their
+// first instruction (at most PCG3_BODY - 1 of them).  Iterations left over below the budget,
+// and solves whose per-launch timing is requested, run as plain launches in chunks of
+// PCG3_CHUNK iterations.
+constexpr int PCG3_BODY = 4, PCG3_CHUNK = 32;
 
-// drops the captured PCG chunk (its kernels hold the preconditioner's buffers)
+// flag[0]: converged, flag[3]: iterations begun, flag[4]: iteration budget
+__global__ void k_pcg_continue(const int* __restrict__ flag, cudaGraphConditionalHandle h) {
+    if (threadIdx.x != 0) return;
+    const volatile int* f = flag;
+    const bool go = f[0] == 0 && f[3] + PCG3_BODY <= f[4];
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// drops the captured PCG graph (its kernels hold the preconditioner's buffers)
 void pcg_graph_reset(fipc_ctx* c) {
     if (c->pcg3_exec) cudaGraphExecDestroy((cudaGraphExec_t)c->pcg3_exec);
     c->pcg3_exec = nullptr;
     c->pcg3_sig.clear();
 }
 
-// a graph of PCG3_CHUNK iterations (SpMV, update, coarse correction) for these kernel
-// arguments, captured on the context's private stream and replayed on the caller's; reused
-// while the arguments (buffers, sizes) stay the same; false when capture is unavailable
+// the while-loop graph for these kernel arguments, captured on the context's private stream and
+// replayed on the caller's; reused while the arguments (buffers, sizes) stay the same; false when
+// conditional graphs are unavailable
 static bool pcg3_graph(fipc_ctx* c, const PCGArgs& a) {
     std::vector<unsigned char> sig(reinterpret_cast<const unsigned char*>(&a), reinterpret_cast<const unsigned char*>(&a) + sizeof(PCGArgs));
     if (a.mg) sig.insert(sig.end(), reinterpret_cast<const unsigned char*>(a.mg), reinterpret_cast<const unsigned char*>(a.mg) + sizeof(MgArgs));
     if (c->pcg3_exec && c->pcg3_sig == sig) return true;
-    if (c->pcg3_exec) cudaGraphExecDestroy((cudaGraphExec_t)c->pcg3_exec);
-    c->pcg3_exec = nullptr;
-    c->pcg3_sig.clear();
+    pcg_graph_reset(c);
     if (!c->cap_stream) {
         cudaStream_t cs;
         if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) return false;
@@ -533,30 +551,44 @@ static bool pcg3_graph(fipc_ctx* c, const PCGArgs& a) {
     }
     cudaStream_t cs = (cudaStream_t)c->cap_stream;
     const int nb = nblk(c->nV, PCG_THREADS);
-    const long long counted = g_launches.load();   // captured launches run (and count) at replay
-    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return false;
-    for (int k = 0; k < PCG3_CHUNK; ++k) {
-        k_pcg_spmv<<<nb, PCG_THREADS, 0, cs>>>(a);
-        k_pcg_update<<<nb, PCG_THREADS, 0, cs>>>(a);
-        if (a.mg) mg_vcycle(c, a, cs);
-        else if (a.cs_blocks) cs_apply(c, a, cs);
-    }
-    g_launches.store(counted);
     cudaGraph_t g = nullptr;
-    if (cudaStreamEndCapture(cs, &g) != cudaSuccess || !g) {
+    if (cudaGraphCreate(&g, 0) != cudaSuccess) {
         cudaGetLastError();
         return false;
     }
-    cudaGraphExec_t ex = nullptr;
-    const bool ok = cudaGraphInstantiate(&ex, g, 0ull) == cudaSuccess;
+    bool ok = false;
+    do {
+        cudaGraphConditionalHandle h;
+        if (cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault) != cudaSuccess) break;
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) != cudaSuccess) break;
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        const long long counted = g_launches.load();   // captured launches run (and count) at replay
+        if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) break;
+        for (int k = 0; k < PCG3_BODY; ++k) {
+            k_pcg_spmv<<<nb, PCG_THREADS, 0, cs>>>(a);
+            k_pcg_update<<<nb, PCG_THREADS, 0, cs>>>(a);
+            if (a.mg) mg_vcycle(c, a, cs);
+            else if (a.cs_blocks) cs_apply(c, a, cs);
+        }
+        k_pcg_continue<<<1, 32, 0, cs>>>(a.flag, h);
+        g_launches.store(counted);
+        cudaGraph_t captured = nullptr;
+        if (cudaStreamEndCapture(cs, &captured) != cudaSuccess || captured != body) break;
+        cudaGraphExec_t ex = nullptr;
+        if (cudaGraphInstantiate(&ex, g, 0ull) != cudaSuccess) break;
+        c->pcg3_exec = ex;
+        c->pcg3_sig = sig;
+        ok = true;
+    } while (false);
     cudaGraphDestroy(g);
-    if (!ok) {
-        cudaGetLastError();
-        return false;
-    }
-    c->pcg3_exec = ex;
-    c->pcg3_sig = sig;
-    return true;
+    if (!ok) cudaGetLastError();
+    return ok;
 }
 
 // solve_system (NEWTON_IPC.py:750-777) by block-Jacobi PCG; sol: device [3 nV] holding the
@@ -565,7 +597,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
               cudaStream_t s) {
     const long long n3 = 3ll * c->nV;
     const int nb = nblk(c->nV, PCG_THREADS);
-    if (c->pcg_vec.ensure(8 * (n3 * 4 + 13ll * c->nV) + 64) || c->pcg_part.ensure(8ll * (3 * nb + SC_COUNT) + 64) || c->scal.ensure(64))
+    if (c->pcg_vec.ensure(8 * (n3 * 4 + 13ll * c->nV) + 64) || c->pcg_part.ensure(8ll * (3 * nb + SC_COUNT) + 64) || c->scal.ensure(80))
         return FIPC_ERR_CUDA;
     if (c->c_nnzb == 0 && (c->c_rowptr.ensure(4ll * (c->nV + 1)) || cudaMemsetAsync(c->c_rowptr.p, 0, 4ll * (c->nV + 1), s)))
         return FIPC_ERR_CUDA;
@@ -592,7 +624,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     a.part = c->pcg_part.as<double>();
     a.sc = a.part + 3 * nb;
     a.flag = (int*)(c->scal.as<char>() + 48);
-    FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 4 * sizeof(int), s));
+    FIPC_CUDA(cudaMemsetAsync(a.flag, 0, 5 * sizeof(int), s));
     int st = c->mg ? mg_prepare(c, fixed, a, s) : cs_prepare(c, fixed, a, s);
     if (st) return st;
     if (a.mg) a.cs_blocks = 0;
@@ -603,7 +635,7 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     const double spmv_flops = (double)(c->nnzb + c->c_nnzb) * 18.0 + nv * 18.0;
     const double upd_bytes = nv * (32.0 * 2 + 24.0 * 2 * 4 + 24.0 + 72.0);
     const double upd_flops = nv * 36.0;
-    k_pcg_start<<<nb, PCG_THREADS, 0, s>>>(a, c->rhs, rtol);
+    k_pcg_start<<<nb, PCG_THREADS, 0, s>>>(a, c->rhs, rtol, maxit);
     FIPC_LAUNCHED();
     if (a.mg) {
         st = mg_start(c, a, s);
@@ -611,40 +643,41 @@ int pcg_solve(fipc_ctx* c, const unsigned char* fixed, const int* /*diag_pos*/, 
     } else if (a.cs_blocks) {
         cs_apply(c, a, s);
     }
-    int h_flag[2] = {0, 0};
-    // per-launch timing of the SpMV or the update needs plain launches; otherwise whole chunks of
-    // iterations replay from a captured graph (one launch per chunk instead of four per iteration)
+    int h_flag[4] = {0, 0, 0, 0};
+    // per-launch timing of the SpMV or the update needs plain launches; otherwise the iterations
+    // replay from the captured while-loop graph, and only a remainder below the budget runs plainly
     const int pk = profile_kernel();
     const bool timed = pk == PK_PCG_SPMV || pk == PK_PCG_UPDATE;
-    const bool graph = !timed && maxit >= PCG3_CHUNK && pcg3_graph(c, a);
     const int per_iter = a.mg ? 2 + mg_launches_per_cycle(c->mg_levels) : (a.cs_blocks ? 4 : 2);
     int k0 = 0;
-    while (k0 < maxit) {
-        if (graph && k0 + PCG3_CHUNK <= maxit) {
-            FIPC_CUDA(cudaGraphLaunch((cudaGraphExec_t)c->pcg3_exec, s));
-            g_launches.fetch_add(PCG3_CHUNK * per_iter, std::memory_order_relaxed);
-            k0 += PCG3_CHUNK;
-        } else {
-            const int k1 = (k0 + PCG3_CHUNK < maxit) ? k0 + PCG3_CHUNK : maxit;
-            for (int k = k0; k < k1; ++k) {
-                {
-                    ProfScope ps(PK_PCG_SPMV, s, spmv_bytes, spmv_flops);
-                    k_pcg_spmv<<<nb, PCG_THREADS, 0, s>>>(a);
-                }
-                FIPC_LAUNCHED();
-                {
-                    ProfScope ps(PK_PCG_UPDATE, s, upd_bytes, upd_flops);
-                    k_pcg_update<<<nb, PCG_THREADS, 0, s>>>(a);
-                }
-                FIPC_LAUNCHED();
-                if (a.mg) mg_vcycle(c, a, s);
-                else if (a.cs_blocks) cs_apply(c, a, s);
-            }
-            k0 = k1;
-        }
-        FIPC_CUDA(cudaMemcpyAsync(h_flag, a.flag, sizeof(int) * 2, cudaMemcpyDeviceToHost, s));
+    if (!timed && maxit >= PCG3_BODY && pcg3_graph(c, a)) {
+        FIPC_CUDA(cudaGraphLaunch((cudaGraphExec_t)c->pcg3_exec, s));
+        FIPC_CUDA(cudaMemcpyAsync(h_flag, a.flag, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
         FIPC_CUDA(cudaStreamSynchronize(s));
-        if (h_flag[0]) break;
+        // bodies run: up to and including the one that saw convergence, else whole budget-sized ones
+        const long long bodies = h_flag[0] ? h_flag[3] / PCG3_BODY + 1 : h_flag[3] / PCG3_BODY;
+        g_launches.fetch_add(bodies * (PCG3_BODY * per_iter + 1), std::memory_order_relaxed);
+        k0 = h_flag[3];
+    }
+    while (!h_flag[0] && k0 < maxit) {
+        const int k1 = (k0 + PCG3_CHUNK < maxit) ? k0 + PCG3_CHUNK : maxit;
+        for (int k = k0; k < k1; ++k) {
+            {
+                ProfScope ps(PK_PCG_SPMV, s, spmv_bytes, spmv_flops);
+                k_pcg_spmv<<<nb, PCG_THREADS, 0, s>>>(a);
+            }
+            FIPC_LAUNCHED();
+            {
+                ProfScope ps(PK_PCG_UPDATE, s, upd_bytes, upd_flops);
+                k_pcg_update<<<nb, PCG_THREADS, 0, s>>>(a);
+            }
+            FIPC_LAUNCHED();
+            if (a.mg) mg_vcycle(c, a, s);
+            else if (a.cs_blocks) cs_apply(c, a, s);
+        }
+        k0 = k1;
+        FIPC_CUDA(cudaMemcpyAsync(h_flag, a.flag, sizeof(int) * 4, cudaMemcpyDeviceToHost, s));
+        FIPC_CUDA(cudaStreamSynchronize(s));
     }
     FIPC_CUDA(cudaGetLastError());
     if (iters) *iters = h_flag[0] ? h_flag[1] : maxit;

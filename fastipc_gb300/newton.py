@@ -154,6 +154,10 @@ class NewtonIPC:
         off; h is the first aggregation box's cell (0: the spatial hash's)."""
         check(N.lib().fipc_ctx_set_multigrid(self.ctx, int(bool(on)), D(h)), 'fipc_ctx_set_multigrid')
 
+    def set_multigrid_fp32(self, on=True):
+        """FP32 level-0 smoothing products in the multigrid V-cycle (on, the default) or FP64 (off)."""
+        check(N.lib().fipc_ctx_set_multigrid_fp32(self.ctx, int(bool(on))), 'fipc_ctx_set_multigrid_fp32')
+
     def multigrid(self):
         """Levels of the multigrid hierarchy in use (0: off) and nodes per level."""
         lv, nodes = ctypes.c_int(), (ctypes.c_int * 8)()

@@ -97,8 +97,16 @@ int fipc_ctx_preconditioner(fipc_ctx* ctx, int* agg_rows, int* n_coarse);
  * off) and nodes per level (nodes_h: 8 ints, may be NULL). */
 int fipc_ctx_set_multigrid(fipc_ctx* ctx, int on, double h);
 int fipc_ctx_multigrid(fipc_ctx* ctx, int* levels, int* nodes_h);
+/* Precision of the V-cycle's two level-0 smoothing products (the residual after pre-smoothing
+ * and the post-smoothing product): 1 = FP32 copies of the values and of the iterate with FP32
+ * sums, the residuals and the smoother updates in FP64 (the default); 0 = FP64.  The PCG's own
+ * product, its recurrences and the coarser levels are FP64 either way; the solve's tolerance is
+ * unchanged. */
+int fipc_ctx_set_multigrid_fp32(fipc_ctx* ctx, int on);
 /* In-place inverse of a dense SPD matrix on the device (n a multiple of 32, row-major; work: 1024
- * + 64 n doubles): the blocked Gauss-Jordan used for the coarse matrix, one cooperative launch. */
+ * + 64 n doubles): the symmetric block sweep (Gauss-Jordan sweep operator on the lower triangle's
+ * 32 x 32 tiles) used for the coarse matrices, one cooperative launch; the result is exactly
+ * symmetric. */
 int fipc_dense_spd_inverse(int n, double* a, double* work, void* stream);
 
 /* find_constraints, NEWTON_IPC.py:337-357 (spatial hash :213-334, dedup :348-356): the seven

@@ -99,6 +99,15 @@ void hc_seg_tri(int count, const double* pts, int* hit) {
     }
 }
 
+// the step filter's early-out for tets (1: the tet is skipped)
+void hc_inversion_skip(int count, const double* xs, const double* ps, double eta, int* skip) {
+    for (int c = 0; c < count; ++c) {
+        v3 X[4], P[4];
+        for (int k = 0; k < 4; ++k) { X[k] = load3(xs + 12 * c, k); P[k] = load3(ps + 12 * c, k); }
+        skip[c] = inversion_cannot_flip(X, P, eta);
+    }
+}
+
 void hc_inversion(int count, const double* xs, const double* ps, double eta, double* out) {
     for (int c = 0; c < count; ++c) {
         v3 X[4], P[4];

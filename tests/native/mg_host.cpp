@@ -223,6 +223,20 @@ void mg_host_plan(int nV, const double* x0, const int* rp, const int* ci, double
     }
 }
 
+// level-1 aggregates: rot[a] (1: rotations, 0: translations only) and member counts; returns
+// the number of aggregates
+int mg_host_level1(int nV, const double* x0, const int* rp, const int* ci, double h, int* rot, int* members) {
+    MgPlan P;
+    mg_build(nV, x0, rp, ci, h, P);
+    if (P.levels < 2) return 0;
+    const MgLevelPlan& c = P.L[1];
+    for (int a = 0; a < c.n; ++a) {
+        rot[a] = c.rot[a];
+        members[a] = c.mem_ptr[a + 1] - c.mem_ptr[a];
+    }
+    return c.n;
+}
+
 // MG-preconditioned CG on the Dirichlet-edited block system (blocks row-major, vertex BSR);
 // x: current positions (the rigid modes' offsets), x0: rest positions (the aggregation).
 // Returns the iteration count (-1: no convergence); info[0..] = omega per level.
@@ -256,7 +270,8 @@ int mg_host_pcg(int nV, const int* rp, const int* ci, const double* ev, const in
         }
         c.d.assign(3 * (size_t)f.n, 0.0);
         for (int i = 0; i < f.n; ++i)
-            for (int q = 0; q < 3; ++q) c.d[3 * i + q] = fp[3 * (size_t)i + q] - c.cent[3 * (size_t)pl.agg_of[i] + q];
+            if (pl.rot.empty() || pl.rot[pl.agg_of[i]])   // translation-only aggregates keep zero offsets
+                for (int q = 0; q < 3; ++q) c.d[3 * i + q] = fp[3 * (size_t)i + q] - c.cent[3 * (size_t)pl.agg_of[i] + q];
         for (int pass = 0; pass < 2; ++pass) {
             const MgPattern& pt = pass ? pl.C : pl.S;
             Vec& out = pass ? c.C : c.S;

@@ -162,3 +162,29 @@ def test_inversion_free(hc, unit_golden):
     out = np.zeros(len(xs))
     hc.hc_inversion(len(xs), P(xs), P(ps), ctypes.c_double(0.2), P(out))
     assert np.abs(out - g['cubic_t']).max() < 1e-6
+
+
+@pytest.mark.parametrize('eta', [0.1, 0.2])
+def test_inversion_early_out_is_exact(hc, unit_golden, eta):
+    """A tet whose volume polynomial provably stays positive over the step's range is skipped:
+    every skipped tet's inversion-free step is >= 1 (golden cases and 40k random tets with
+    vertex motions from 1e-4 to 3 of the tet's size)."""
+    g = unit_golden
+    rng = np.random.default_rng(5)
+    n = 40000
+    X = rng.normal(size=(n, 4, 3))
+    vol = np.einsum('ij,ij->i', np.cross(X[:, 1] - X[:, 0], X[:, 2] - X[:, 0]), X[:, 3] - X[:, 0])
+    X[vol < 0, 3] = 2 * X[vol < 0, 0] - X[vol < 0, 3]      # positive orientation
+    rs = 10.0 ** rng.uniform(-4, 0.5, size=n)
+    Pm = rng.normal(size=(n, 4, 3)) * rs[:, None, None] + rng.normal(size=(n, 1, 3))
+    xs = np.ascontiguousarray(np.concatenate([np.reshape(g['cubic_x'], (-1, 12)), X.reshape(n, 12)]))
+    ps = np.ascontiguousarray(np.concatenate([np.reshape(g['cubic_p'], (-1, 12)), Pm.reshape(n, 12)]))
+    out = np.zeros(len(xs))
+    skip = np.zeros(len(xs), np.int32)
+    hc.hc_inversion(len(xs), P(xs), P(ps), ctypes.c_double(eta), P(out))
+    hc.hc_inversion_skip(len(xs), P(xs), P(ps), ctypes.c_double(eta), P(skip))
+    s = skip.astype(bool)
+    assert np.all(out[s] >= 1.0)
+    small = np.concatenate([np.zeros(len(xs) - n, bool), rs < 1e-2])
+    assert s[small].mean() > 0.5
+    assert (out[~s] < 1.0).any()

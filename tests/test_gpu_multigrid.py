@@ -72,3 +72,26 @@ def test_multigrid_direction_vs_two_level(case):
         assert p_again.tobytes() == p_mg.tobytes()
     finally:
         sim.close()
+
+
+@pytest.mark.parametrize('case', ['bar', 'lattice'])
+def test_fp32_smoothing_products(case):
+    """FP32 level-0 smoothing products (the default): the same direction as the FP64 cycle (1e-8
+    of its largest entry at relative residual 1e-12), at most 10% more PCG iterations, bitwise
+    reproducible."""
+    sim, f = _state(case)
+    try:
+        sim.set_multigrid_fp32(False)
+        p64, it64 = _solve(sim, f)
+        sim.set_multigrid_fp32(True)
+        p32, it32 = _solve(sim, f)
+        p32b, _ = _solve(sim, f)
+        assert p32.tobytes() == p32b.tobytes()
+        assert np.abs(p32 - p64).max() <= 1e-8 * np.abs(p64).max()
+        assert it32 <= 1.1 * it64 + 2, (it32, it64)
+        sim.set_multigrid_fp32(False)
+        p64b, _ = _solve(sim, f)
+        assert p64b.tobytes() == p64.tobytes()
+        sim.set_multigrid_fp32(True)
+    finally:
+        sim.close()

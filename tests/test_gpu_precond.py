@@ -70,9 +70,10 @@ def test_full_step_matches_block_jacobi():
     b.close()
 
 
-@pytest.mark.parametrize('n', [32, 96, 544])
+@pytest.mark.parametrize('n', [32, 96, 544, 800])
 def test_dense_spd_inverse(n):
-    """the blocked Gauss-Jordan inverse of the coarse solve against numpy (1e-10 relative)"""
+    """the symmetric block-sweep inverse of the coarse solves against numpy (1e-10 relative),
+    exactly symmetric"""
     import ctypes
     import torch
     from fastipc_gb300 import _native as NN
@@ -83,5 +84,7 @@ def test_dense_spd_inverse(n):
     work = torch.empty(1024 + 64 * n, dtype=torch.float64, device='cuda')
     assert NN.lib().fipc_dense_spd_inverse(n, ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(work.data_ptr()), NN.stream()) == 0
     ref = np.linalg.inv(A)
-    assert np.abs(d.cpu().numpy() - ref).max() <= 1e-10 * np.abs(ref).max()
+    out = d.cpu().numpy()
+    assert np.abs(out - ref).max() <= 1e-10 * np.abs(ref).max()
+    assert np.array_equal(out, out.T)
     assert NN.lib().fipc_dense_spd_inverse(100, ctypes.c_void_p(d.data_ptr()), ctypes.c_void_p(work.data_ptr()), NN.stream()) != 0

@@ -118,3 +118,24 @@ def test_aggregates_stay_inside_bodies(mg):
     cubes = 8 + 1
     assert n1 >= cubes            # at least one aggregate per body
     assert nnz1 <= 27 * n1        # a box neighbourhood per row
+
+
+def test_line_aggregates_keep_translations_only(mg):
+    """Level-1 aggregates of one or two vertices, or of collinear vertices, have a rank-deficient
+    rotation block (the rotation about their line moves nothing): the plan keeps their
+    translations only.  Every other aggregate keeps its rotations; on the two-cube scene, whose
+    box grid leaves single vertices and vertex pairs at the cubes' edges, both kinds occur."""
+    scene = scenes.predeform(scenes.two_cubes(n=8, seed=1), 2e-4, 1)
+    A, rhs, mask, x = _system(scene)
+    rp, ci, _ = _bsr(A)
+    x0 = np.ascontiguousarray(scene.x, dtype=np.float64)
+    be = scene.boundary_edges
+    h = float(np.median(np.linalg.norm(x0[be[:, 0]] - x0[be[:, 1]], axis=1)))
+    rot = np.zeros(len(x0), np.int32)
+    mem = np.zeros(len(x0), np.int32)
+    n = mg.mg_host_level1(len(x0), P(x0), P(rp), P(ci), ctypes.c_double(h), P(rot), P(mem))
+    rot, mem = rot[:n], mem[:n]
+    assert n > 0
+    assert np.all(rot[mem <= 2] == 0)
+    assert np.all(mem[rot == 0] <= 9)          # only thin slivers lose their rotations
+    assert (rot == 1).sum() > 0.8 * n
